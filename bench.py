@@ -1,0 +1,365 @@
+"""Benchmark: Ax=b GFLOP/s at backward error <= n*eps64 on one GB300.
+
+Workload (default): plain FP64 getrf + getrs, n = 16384, 16 right-hand sides,
+A and B iid N(0, 1) from a seeded Philox generator (synthetic; no dataset
+exists for this metric).  One step = restore A and B in HBM, factor, solve.
+GFLOP/s = (2/3 n^3 + 2 n^2 nrhs) / time.  The solution's normwise backward
+error ||b - Ax||_inf / (||A||_inf ||x||_inf + ||b||_inf) is checked against
+n * 2^-53 after the timed steps.
+
+Printed as one JSON line (rank 0):
+  value     device-resident throughput (inputs in HBM when timing starts)
+  e2e       the same solve through the C ABI with host buffers
+            (luhot_dgesv: A, B copied in and X copied out every step)
+  roofline  the Schur-update GEMM (the dominant kernel) against the FP64
+            tensor-core peak measured in this run
+  cpu_baseline  lair's algorithm (the CPU oracle) on a bounded sample
+  ir        mixed-precision LU + iterative refinement on the kappa-conditioned
+            n = 16384 system, when built
+
+--impl reference times lair's own algorithm on the host cores instead (the
+oracle port: lair is Rust and cannot be built here).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Ax=b GFLOP/s at backward err ≤ n·eps64: FP64 LU vs mixed-precision IR, 1 GB300"
+EPS64 = 2.0 ** -53
+
+
+def flops_of(n: int, nrhs: int) -> float:
+    return 2.0 / 3.0 * n ** 3 + 2.0 * n * n * nrhs
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            if self.thread:
+                self.thread.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------
+# CPU baseline: lair's getrf_row_major + getrs (the oracle) on a bounded
+# slice of the same n x n system, one core (lair is single-threaded).
+# --------------------------------------------------------------------------
+def cpu_sample(n: int, seed: int, elim_steps: int, state=None):
+    """Run `elim_steps` elimination steps (continuing from `state`) and one
+    single-RHS getrs; returns (flops, seconds, state)."""
+    import oracle
+
+    if state is None:
+        rng = np.random.default_rng(seed)
+        a = rng.standard_normal((n, n))
+        b = rng.standard_normal(n)
+        piv = np.arange(n, dtype=np.uint64)
+        state = {"a": a, "b": b, "piv": piv, "next": 0}
+    a, piv, b = state["a"], state["piv"], state["b"]
+    s0 = state["next"]
+    s1 = min(n, s0 + elim_steps)
+    fl = 0.0
+    for ul in range(s0, s1):
+        r = n - ul - 1
+        fl += r + 2.0 * r * r  # scale + rank-1 update
+    t0 = time.perf_counter()
+    oracle.getrf_row_major_range(a, piv, s0, s1)
+    t1 = time.perf_counter()
+    oracle.getrs(a, piv, b)  # cost of one getrs does not depend on the values
+    t2 = time.perf_counter()
+    fl += 2.0 * n * n
+    state["next"] = s1
+    return fl, (t2 - t0), state
+
+
+def cpu_baseline(n: int, seconds: float = 12.0):
+    fl_total, t_total, steps, state = 0.0, 0.0, 0, None
+    while t_total < seconds and (state is None or state["next"] < n):
+        fl, t, state = cpu_sample(n, 1234, 2, state)
+        fl_total += fl
+        t_total += t
+        steps += 1
+    return {"value": fl_total / t_total / 1e9, "unit": "GFLOP/s", "cores": 1, "kind": "port",
+            "sample": (f"lair getrf_row_major + getrs restated in C++ (-O2 -ffp-contract=off), 1 thread: "
+                       f"the first {state['next']} elimination steps of an n={n} N(0,1) matrix plus "
+                       f"{steps} single-RHS getrs at n={n}; {t_total:.1f} s of CPU work"),
+            "host": os.uname().machine, "host_cores_total": os.cpu_count()}
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    n = args.n
+    state = None
+    for _ in range(args.warmup):
+        _, _, state = cpu_sample(n, 1234, args.ref_elim_steps, state)
+    fl_total, t_total = 0.0, 0.0
+    for _ in range(args.steps):
+        fl, t, state = cpu_sample(n, 1234, args.ref_elim_steps, state)
+        fl_total += fl
+        t_total += t
+    value = fl_total / t_total / 1e9
+    sample = (f"each step: {args.ref_elim_steps} elimination steps of lair's getrf_row_major on the n={n} "
+              f"N(0,1) matrix (continuing) + one single-RHS getrs at n={n}; oracle port in C++, 1 thread "
+              f"(lair is single-threaded)")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "GFLOP/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_total / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": workload_config(args),
+            "cpu_baseline": {"value": value, "unit": "GFLOP/s", "cores": 1, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(args):
+    return {"workload": f"plain FP64 getrf+getrs drop-in, n={args.n}, nrhs={args.nrhs}, A,B iid N(0,1) seeded",
+            "n": args.n, "nrhs": args.nrhs, "mode": args.mode,
+            "l2": "inputs larger than L2 (A is %.1f GiB vs 129 MB L2)" % (args.n * args.n * 8 / 2 ** 30),
+            "parallelism": "replicas (one independent system per GPU)"}
+
+
+def read_traffic(path):
+    """Per-launch DRAM traffic of the GEMM from a committed ncu summary, if any."""
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].strip())
+    except OSError:
+        pass
+    return None
+
+
+def run_ours(args):
+    import ctypes
+
+    import torch
+
+    from lair_gb300 import _lib
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    lib = _lib.load()
+    ctx = _lib.context() if local == 0 else None
+    if ctx is None:  # one context per process, on this process's GPU
+        h = ctypes.c_void_p()
+        _lib.check(lib.luhot_create(ctypes.byref(h), local))
+        ctx = h
+        _lib._ctx = ctx
+    # One explicit stream for torch's copies and luhot's kernels (the legacy
+    # default stream would not order against luhot's non-blocking stream).
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    _lib.check(lib.luhot_set_stream(ctx, ctypes.c_void_p(stream.cuda_stream)), ctx)
+    mode = _lib.mode_id(args.mode)
+
+    n, nrhs = args.n, args.nrhs
+    lda = n
+    gen = torch.Generator(device="cuda").manual_seed(args.seed + rank)
+    A0 = torch.randn((n, n), dtype=torch.float64, device="cuda", generator=gen)
+    B0 = torch.randn((n, nrhs), dtype=torch.float64, device="cuda", generator=gen)
+    A = torch.empty_like(A0)
+    X = torch.empty_like(B0)
+    piv = torch.empty(n, dtype=torch.int32, device="cuda")
+    sing = ctypes.c_int64(0)
+
+    peak = _lib.dmma_peak_tflops()
+
+    def step():
+        A.copy_(A0)
+        X.copy_(B0)
+        _lib.check(lib.luhot_dgetrf_dev(ctx, n, n, A.data_ptr(), lda, piv.data_ptr(), ctypes.byref(sing), mode), ctx)
+        _lib.check(lib.luhot_dgetrs_dev(ctx, n, nrhs, A.data_ptr(), lda, piv.data_ptr(), X.data_ptr(), nrhs, 0, mode), ctx)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    _lib.profile_enable(True)
+    launches0 = lib.luhot_launch_count(ctx)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        barrier()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+        ev1.record(stream)
+        barrier()
+    launches = lib.luhot_launch_count(ctx) - launches0
+    prof = _lib.profile_read()
+    _lib.profile_enable(False)
+    ms = ev0.elapsed_time(ev1)
+    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = world * args.steps * flops_of(n, nrhs) / (ms_max * 1e-3) / 1e9
+
+    # backward error of the last solve (FP64 on the GPU)
+    R = B0 - A0 @ X
+    berr = (R.abs().max() / (A0.abs().sum(1).max() * X.abs().max() + B0.abs().max())).item()
+
+    g = prof.get("gemm", {"ms": 0.0, "flops": 0.0, "launches": 0})
+    gemm_tflops = g["flops"] / (g["ms"] * 1e-3) / 1e12 if g["ms"] else 0.0
+    traffic = read_traffic(os.path.join(ROOT, "profiles", "gemm_dmma_fp64_n16384.md"))
+    total_prof_ms = sum(v["ms"] for v in prof.values())
+    roofline = {"bound": "tensor", "achieved": gemm_tflops, "peak": peak, "unit": "TFLOP/s",
+                "frac": gemm_tflops / peak if peak else None, "traffic": traffic,
+                "kernel": "gemm_dmma_kernel (FP64 Schur update, mma.sync m8n8k4)",
+                "peak_source": "FP64 DMMA throughput measured in this run (register-resident "
+                               "mma.sync m8n8k4 loop); MEASURED_PEAKS.json has no FP64 figure",
+                "per_launch_flops": g["flops"] / max(1, g["launches"]),
+                "launches": g["launches"], "share_of_step": g["ms"] / total_prof_ms if total_prof_ms else None,
+                "overall_frac_of_peak": (flops_of(n, nrhs) * args.steps / (ms_max * 1e-3) / 1e12) / peak
+                if peak else None}
+
+    # e2e: equation::solve through the C ABI with host buffers every step
+    e2e = None
+    if not args.no_e2e:
+        A_h = A0.cpu().numpy()
+        B_h = B0.cpu().numpy()
+        X_h = np.empty_like(B_h)
+        _lib.check(lib.luhot_set_stream(ctx, None), ctx)
+
+        def e2e_step():
+            rc = lib.luhot_dgesv(ctx, n, nrhs, A_h.ctypes.data, n, 1, B_h.ctypes.data, nrhs, 1,
+                                 X_h.ctypes.data, nrhs, 1, mode)
+            _lib.check(rc, ctx)
+
+        for _ in range(max(1, min(args.warmup, 2))):
+            e2e_step()
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        barrier()
+        dt = time.perf_counter() - t0
+        tt = torch.tensor([dt], dtype=torch.float64, device="cuda")
+        if world > 1:
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        dt = float(tt.item())
+        e2e = {"value": world * args.steps * flops_of(n, nrhs) / dt / 1e9, "unit": "GFLOP/s",
+               "h2d_bytes_per_step": int(A_h.nbytes + B_h.nbytes), "d2h_bytes_per_step": int(X_h.nbytes),
+               "api": "luhot_dgesv (host A, B in; host X out; pageable numpy buffers)",
+               "ms_per_step": dt / args.steps * 1e3}
+        _lib.check(lib.luhot_set_stream(ctx, ctypes.c_void_p(stream.cuda_stream)), ctx)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline(n, args.cpu_seconds)
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "GFLOP/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": workload_config(args), "backward_error": berr, "berr_bound": n * EPS64,
+                "berr_ok": berr <= n * EPS64, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "clocks": clocks.summary(), "gpu_launches": int(launches),
+                "kernel_profile_ms": {k: round(v["ms"], 3) for k, v in prof.items()}}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=16384)
+    ap.add_argument("--nrhs", type=int, default=16)
+    ap.add_argument("--mode", choices=["fast", "exact"], default="fast")
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--ref-elim-steps", type=int, default=4)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

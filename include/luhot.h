@@ -1,0 +1,146 @@
+/*
+ * luhot: GB300-native (sm_103a) LU hot path of lair, behind a C ABI.
+ *
+ * These entry points are what lair's Rust shim would bind (through an
+ * `extern "C"` crate) from inside `lapack::getrf` / `lapack::getrs` for f64
+ * and f32, selected by `TypeId::of::<A>()`; every other element type keeps
+ * lair's own code.  Citations name the lair 0.8.0 function each entry point
+ * replaces (paths inside lair's source tree).
+ *
+ * Conventions shared by every call:
+ *  - Every function returns an int status (LUHOT_OK == 0).  A failed call
+ *    leaves a message in luhot_last_error(ctx).  No call aborts the process.
+ *  - Host matrices are described by a pointer to element (0, 0) and signed
+ *    element strides (rs = row stride, cs = column stride).  Negative strides
+ *    and any layout an ndarray view can have are accepted.  Caller memory is
+ *    never freed or retained after the call returns.
+ *  - Pivots are 0-based LAPACK-style sequential interchanges, as lair returns
+ *    them: at step i, row i was swapped with row piv[i] (piv[i] >= i).
+ *  - `singular` mirrors lair's Option<usize>: -1 is None, otherwise the LAST
+ *    elimination step whose pivot column was all zero.
+ *  - mode LUHOT_MODE_EXACT reproduces lair's operation order bit for bit
+ *    (row-major getrf order, src/lapack/getrf.rs:46-120, and getrs order,
+ *    src/lapack/getrs.rs:12-38); LUHOT_MODE_FAST uses the FP64 tensor cores
+ *    and FMA, with identical pivots wherever the pivot candidates are
+ *    distinct and a backward error of the same order.
+ *  - A context is safe to share between threads: calls on one context are
+ *    serialised by a mutex.  Use one context per thread for concurrency.
+ */
+#ifndef LUHOT_H
+#define LUHOT_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+#define LUHOT_OK 0
+#define LUHOT_ERR_INVALID_ARG 1   /* shape / stride / null-pointer error */
+#define LUHOT_ERR_CUDA 2          /* a CUDA runtime call failed */
+#define LUHOT_ERR_ALLOC 3         /* device or pinned allocation failed */
+#define LUHOT_ERR_TIMEOUT 4       /* a device-side bounded wait gave up */
+#define LUHOT_ERR_NOT_CONVERGED 5 /* iterative refinement did not reach tol */
+#define LUHOT_ERR_SINGULAR 6      /* a solve met an exactly singular factor */
+#define LUHOT_ERR_UNSUPPORTED 7   /* size or option outside what is built */
+
+/* Arithmetic modes. */
+#define LUHOT_MODE_FAST 0
+#define LUHOT_MODE_EXACT 1
+
+typedef struct luhot_ctx luhot_ctx;
+
+/* Library version string, e.g. "0.1.0". */
+const char* luhot_version(void);
+/* Human-readable name of a status code. */
+const char* luhot_status_string(int status);
+
+/* Create a context on `device` (its own CUDA stream and workspace). */
+int luhot_create(luhot_ctx** out, int device);
+/* Release a context and its device memory.  NULL is accepted. */
+void luhot_destroy(luhot_ctx* ctx);
+/* Message of the last failed call on this context ("" if none). */
+const char* luhot_last_error(const luhot_ctx* ctx);
+/* Run subsequent calls on a caller-owned cudaStream_t (NULL: own stream). */
+int luhot_set_stream(luhot_ctx* ctx, void* cuda_stream);
+/* Panel width override (0 = default 64); for tuning and tests. */
+int luhot_set_block(luhot_ctx* ctx, int nb);
+/* Kernel launches issued by this context since creation. */
+int64_t luhot_launch_count(const luhot_ctx* ctx);
+/* Self-test of the device-side wait limit: launches two CTAs that wait on a
+ * grid barrier nothing completes, with the given limit (1..10000 ms).
+ * Returns LUHOT_ERR_TIMEOUT and leaves the context usable.  No lair
+ * counterpart (lair has no device waits). */
+int luhot_selftest_wait_timeout(luhot_ctx* ctx, int64_t timeout_ms);
+
+/* Per-kernel-class CUDA-event profile (no lair counterpart).  Classes:
+ * 0 panel, 1 laswp, 2 trsm, 3 Schur GEMM, 4 triangular solve (getrs),
+ * 5 permutation, 6 refinement (residual / update), 7 other.  flops and
+ * bytes are the algorithmic work of the timed launches. */
+typedef struct luhot_profile {
+  double ms[8];
+  double flops[8];
+  double bytes[8];
+  int64_t launches[8];
+} luhot_profile;
+/* Enable (1) or disable (0) event bracketing; clears what was recorded. */
+int luhot_profile_enable(luhot_ctx* ctx, int on);
+/* Synchronise, sum the recorded launches per class into *out, and clear. */
+int luhot_profile_read(luhot_ctx* ctx, luhot_profile* out);
+/* Measured FP64 tensor-core (DMMA, mma.sync m8n8k4) throughput of this GPU
+ * in TFLOP/s, from a register-resident kernel with no memory traffic; the
+ * denominator of the FP64 roofline fraction. */
+int luhot_measure_dmma_peak(luhot_ctx* ctx, double* tflops);
+
+/* ---- Host-buffer (drop-in) entry points ------------------------------- */
+
+/* LU with partial pivoting of an m x n matrix, in place (the caller's array
+ * becomes L\U, in its own layout).  piv receives min(m, n) entries.
+ * Replaces lapack::getrf, src/lapack/getrf.rs:12-27 (and through it
+ * getrf_row_major :46-120 / getrf_col_major :128-213). */
+int luhot_dgetrf(luhot_ctx* ctx, int64_t m, int64_t n, double* a, int64_t rs, int64_t cs,
+                 uint64_t* piv, int64_t* singular, int mode);
+int luhot_sgetrf(luhot_ctx* ctx, int64_t m, int64_t n, float* a, int64_t rs, int64_t cs,
+                 uint64_t* piv, int64_t* singular, int mode);
+
+/* Solve A X = B (trans = 0) or A^T X = B (trans = 1) for nrhs right-hand
+ * sides with the factors of luhot_?getrf: lu is n x ncols (only its first n
+ * columns are read), piv has n entries, B and X are n x nrhs (X may alias B).
+ * Replaces lapack::getrs, src/lapack/getrs.rs:12-38 (one column of B is
+ * lair's single right-hand side; trans = 1 has no lair counterpart and
+ * serves the adjoint). */
+int luhot_dgetrs(luhot_ctx* ctx, int64_t n, int64_t nrhs, const double* lu, int64_t lu_rs,
+                 int64_t lu_cs, const uint64_t* piv, const double* b, int64_t b_rs, int64_t b_cs,
+                 double* x, int64_t x_rs, int64_t x_cs, int trans, int mode);
+int luhot_sgetrs(luhot_ctx* ctx, int64_t n, int64_t nrhs, const float* lu, int64_t lu_rs,
+                 int64_t lu_cs, const uint64_t* piv, const float* b, int64_t b_rs, int64_t b_cs,
+                 float* x, int64_t x_rs, int64_t x_cs, int trans, int mode);
+
+/* One-shot solve of a square system: the work of equation::solve
+ * (src/equation.rs:32-59): factor a copy of A, report singularity
+ * (LUHOT_ERR_SINGULAR, A untouched), else solve for nrhs columns. */
+int luhot_dgesv(luhot_ctx* ctx, int64_t n, int64_t nrhs, const double* a, int64_t rs,
+                int64_t cs, const double* b, int64_t b_rs, int64_t b_cs, double* x, int64_t x_rs,
+                int64_t x_cs, int mode);
+
+/* ---- Device-resident entry points ------------------------------------ */
+/* Matrices are row-major on the device with leading dimension ld (elements);
+ * pivots are int32 on the device.  The call is asynchronous on the context's
+ * stream except where a host output (singular) forces a synchronisation. */
+
+/* In-place LU of a device matrix.  Replaces the same lair code as luhot_dgetrf. */
+int luhot_dgetrf_dev(luhot_ctx* ctx, int64_t m, int64_t n, double* d_a, int64_t lda, int32_t* d_piv,
+                     int64_t* singular, int mode);
+int luhot_sgetrf_dev(luhot_ctx* ctx, int64_t m, int64_t n, float* d_a, int64_t lda, int32_t* d_piv,
+                     int64_t* singular, int mode);
+/* Solve with device factors; B (n x nrhs, ldb) is overwritten by X. */
+int luhot_dgetrs_dev(luhot_ctx* ctx, int64_t n, int64_t nrhs, const double* d_lu, int64_t lda,
+                     const int32_t* d_piv, double* d_b, int64_t ldb, int trans, int mode);
+int luhot_sgetrs_dev(luhot_ctx* ctx, int64_t n, int64_t nrhs, const float* d_lu, int64_t lda,
+                     const int32_t* d_piv, float* d_b, int64_t ldb, int trans, int mode);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LUHOT_H */

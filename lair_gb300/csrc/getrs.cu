@@ -1,0 +1,319 @@
+// Triangular solves with the LU factors (getrs) on one GB300.
+//
+// Layout: LU row-major (lda), right-hand sides row-major n x nrhs (ld).
+// A = P L U with P the product of the sequential interchanges in piv.
+//
+//   trans = 0:  x = U^-1 L^-1 P^T b   (lair's getrs, src/lapack/getrs.rs:12-38)
+//   trans = 1:  x = P L^-T U^-T b     (for the adjoint; no lair counterpart)
+//
+// P^T b is one gather through the permutation that the interchanges compose
+// to (computed once by perm_kernel); P w is the matching scatter.
+//
+// Blocked triangular solves: a diagonal-block kernel (one CTA, sequential per
+// right-hand side) and an update kernel for the rows outside the block (one
+// thread per (row, rhs), the block of A staged in shared memory).
+// In exact mode the forward sweep keeps lair's order (each row subtracts
+// l[i][k] * x[k] for increasing k, multiply and subtract rounded apart).  The
+// backward sweep in lair subtracts u[i][k] * x[k] for k = i+1 .. n-1 in
+// increasing k, which makes every row wait for the row below it and the
+// whole sweep one dependent chain of n^2/2 subtractions; exact mode runs that
+// chain literally (back_exact_kernel, one warp per right-hand side).  Fast
+// mode blocks the backward sweep too and uses FMA.
+#include <algorithm>
+
+#include "common.cuh"
+#include "luhot_internal.h"
+
+namespace luhot {
+
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+
+template <bool kExact>
+__device__ __forceinline__ double sub_prod(double c, double l, double u) {
+  if (kExact) return __dsub_rn(c, __dmul_rn(l, u));
+  return fma(-l, u, c);
+}
+template <bool kExact>
+__device__ __forceinline__ float sub_prod(float c, float l, float u) {
+  if (kExact) return __fsub_rn(c, __fmul_rn(l, u));
+  return fmaf(-l, u, c);
+}
+
+// perm[i] = row of the original vector that lands at position i once the
+// interchanges piv[0..n) are applied in order (the effect of
+// src/lapack/laswp.rs:11-40 on an index vector).
+__global__ void perm_kernel(const int* piv_in, int n, int* perm_out, int use_smem) {
+  extern __shared__ int sbuf[];
+  int* perm = use_smem ? sbuf : perm_out;
+  const int* piv = piv_in;
+  if (use_smem) {
+    int* spiv = sbuf + n;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) spiv[i] = piv_in[i];
+    piv = spiv;
+  }
+  for (int i = threadIdx.x; i < n; i += blockDim.x) perm[i] = i;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < n; ++i) {
+      const int p = piv[i];
+      if (p != i && p >= 0 && p < n) {
+        const int t = perm[i];
+        perm[i] = perm[p];
+        perm[p] = t;
+      }
+    }
+  }
+  __syncthreads();
+  if (use_smem)
+    for (int i = threadIdx.x; i < n; i += blockDim.x) perm_out[i] = perm[i];
+}
+
+// x[i][r] = b[perm[i]][r] (gather) or x[perm[i]][r] = b[i][r] (scatter).
+template <typename T, bool kScatter>
+__global__ void permute_rows_kernel(const T* b, int64_t ldb, T* x, int64_t ldx, const int* perm,
+                                    int n, int nrhs) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)n * nrhs) return;
+  const int i = (int)(t / nrhs), r = (int)(t - (int64_t)i * nrhs);
+  if (kScatter)
+    x[(int64_t)perm[i] * ldx + r] = b[(int64_t)i * ldb + r];
+  else
+    x[(int64_t)i * ldx + r] = b[(int64_t)perm[i] * ldb + r];
+}
+
+constexpr int kTrsvBlock = 64;
+
+// Element (i, k) of op(A): A itself or its transpose.
+template <typename T, bool kTrans>
+__device__ __forceinline__ T op_at(const T* a, int64_t lda, int i, int k) {
+  return kTrans ? a[(int64_t)k * lda + i] : a[(int64_t)i * lda + k];
+}
+
+// Solve the diagonal block [j0, j0+bs) of a triangular op(A) in place in x.
+// kLower: forward, rows ascending; otherwise backward, rows descending.
+// kUnit: unit diagonal (L); otherwise divide by the diagonal (U).
+template <typename T, bool kExact, bool kLower, bool kUnit, bool kTrans>
+__global__ void trsv_diag_kernel(const T* a, int64_t lda, T* x, int64_t ldx, int j0, int bs,
+                                 int nrhs) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* A = reinterpret_cast<T*>(smem_raw);  // [bs][bs]
+  for (int idx = threadIdx.x; idx < bs * bs; idx += blockDim.x) {
+    const int i = idx / bs, k = idx - i * bs;
+    A[idx] = op_at<T, kTrans>(a, lda, j0 + i, j0 + k);
+  }
+  __syncthreads();
+  for (int r = threadIdx.x; r < nrhs; r += blockDim.x) {
+    if (kLower) {
+      for (int i = 0; i < bs; ++i) {
+        T acc = x[(int64_t)(j0 + i) * ldx + r];
+        for (int k = 0; k < i; ++k) acc = sub_prod<kExact>(acc, A[i * bs + k], x[(int64_t)(j0 + k) * ldx + r]);
+        if (!kUnit) acc = acc / A[i * bs + i];
+        x[(int64_t)(j0 + i) * ldx + r] = acc;
+      }
+    } else {
+      for (int i = bs - 1; i >= 0; --i) {
+        T acc = x[(int64_t)(j0 + i) * ldx + r];
+        for (int k = i + 1; k < bs; ++k)
+          acc = sub_prod<kExact>(acc, A[i * bs + k], x[(int64_t)(j0 + k) * ldx + r]);
+        if (!kUnit) acc = acc / A[i * bs + i];
+        x[(int64_t)(j0 + i) * ldx + r] = acc;
+      }
+    }
+  }
+}
+
+// x[i] -= sum_{k in [j0, j0+bs)} op(A)(i, k) x[k] for rows i in [i_begin, i_end),
+// k increasing.  Each CTA stages a 64-row slice of op(A)(:, J) in shared memory.
+template <typename T, bool kExact, bool kTrans>
+__global__ void __launch_bounds__(256) trsv_update_kernel(const T* a, int64_t lda, T* x, int64_t ldx,
+                                                          int j0, int bs, int i_begin, int i_end,
+                                                          int nrhs) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* As = reinterpret_cast<T*>(smem_raw);  // [64][bs + 1]
+  T* Xs = As + 64 * (bs + 1);              // [bs][nrhs]
+  const int row0 = i_begin + blockIdx.x * 64;
+  const int rows = min(64, i_end - row0);
+  if (rows <= 0) return;
+  for (int idx = threadIdx.x; idx < rows * bs; idx += blockDim.x) {
+    int i, k;
+    if (kTrans) {  // coalesce along i: element (i, k) = a[k][i]
+      k = idx / rows;
+      i = idx - k * rows;
+    } else {
+      i = idx / bs;
+      k = idx - i * bs;
+    }
+    As[i * (bs + 1) + k] = op_at<T, kTrans>(a, lda, row0 + i, j0 + k);
+  }
+  for (int idx = threadIdx.x; idx < bs * nrhs; idx += blockDim.x) {
+    const int k = idx / nrhs, r = idx - k * nrhs;
+    Xs[idx] = x[(int64_t)(j0 + k) * ldx + r];
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < rows * nrhs; idx += blockDim.x) {
+    const int i = idx / nrhs, r = idx - i * nrhs;
+    T acc = x[(int64_t)(row0 + i) * ldx + r];
+    for (int k = 0; k < bs; ++k) acc = sub_prod<kExact>(acc, As[i * (bs + 1) + k], Xs[k * nrhs + r]);
+    x[(int64_t)(row0 + i) * ldx + r] = acc;
+  }
+}
+
+// lair's backward substitution, literally (src/lapack/getrs.rs:30-36):
+// for i = n-1 .. 0: for k = i+1 .. n-1: x[i] -= u[i][k] * x[k]; x[i] /= u[i][i].
+// One warp per right-hand side: the lanes form the products of a 32-wide
+// chunk, lane 0 subtracts them in order.  x lives in shared memory when it
+// fits, else in place in global memory.
+template <typename T>
+__global__ void back_exact_kernel(const T* u, int64_t lda, T* x, int64_t ldx, int n, int use_smem) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ T prod[32];
+  T* xs = reinterpret_cast<T*>(smem_raw);
+  const int r = blockIdx.x;
+  const int lane = threadIdx.x;
+  T* xg = x + r;  // column r, stride ldx
+  if (use_smem) {
+    for (int i = lane; i < n; i += 32) xs[i] = xg[(int64_t)i * ldx];
+    __syncwarp();
+  }
+  for (int i = n - 1; i >= 0; --i) {
+    const T* urow = u + (int64_t)i * lda;
+    T acc = use_smem ? xs[i] : xg[(int64_t)i * ldx];
+    for (int k0 = i + 1; k0 < n; k0 += 32) {
+      const int k = k0 + lane;
+      if (k < n) prod[lane] = mul_rn(urow[k], use_smem ? xs[k] : xg[(int64_t)k * ldx]);
+      __syncwarp();
+      if (lane == 0) {
+        const int cnt = min(32, n - k0);
+        for (int q = 0; q < cnt; ++q) acc = acc - prod[q];
+      }
+      __syncwarp();
+    }
+    if (lane == 0) {
+      acc = acc / urow[i];
+      if (use_smem)
+        xs[i] = acc;
+      else
+        xg[(int64_t)i * ldx] = acc;
+    }
+    __syncwarp();
+  }
+  if (use_smem) {
+    for (int i = lane; i < n; i += 32) xg[(int64_t)i * ldx] = xs[i];
+  }
+}
+
+template <typename T>
+static int launch_perm(luhot_ctx* ctx, const int* piv, int n, int* perm, cudaStream_t stream) {
+  const size_t bytes = 2 * (size_t)n * sizeof(int);  // permutation + pivots
+  const int use_smem = bytes <= (size_t)ctx->max_smem_optin ? 1 : 0;
+  const size_t smem = use_smem ? bytes : 0;
+  LUHOT_CUDA_TRY(ctx, cudaFuncSetAttribute(perm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)std::max<size_t>(smem, 0)));
+  prof_begin(ctx, kProfPermute);
+  perm_kernel<<<1, 1024, smem, stream>>>(piv, n, perm, use_smem);
+  prof_end(ctx, kProfPermute, 0.0, 2.0 * n * sizeof(int));
+  LUHOT_CUDA_TRY(ctx, cudaGetLastError());
+  return LUHOT_OK;
+}
+
+template <typename T, bool kExact, bool kLower, bool kUnit, bool kTrans>
+static int blocked_trsv(luhot_ctx* ctx, const T* a, int64_t lda, T* x, int64_t ldx, int n, int nrhs,
+                        cudaStream_t stream) {
+  const int bsz = kTrsvBlock;
+  const size_t diag_smem = (size_t)bsz * bsz * sizeof(T);
+  auto dk = trsv_diag_kernel<T, kExact, kLower, kUnit, kTrans>;
+  LUHOT_CUDA_TRY(ctx, cudaFuncSetAttribute(dk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)diag_smem));
+  const size_t upd_smem = ((size_t)64 * (bsz + 1) + (size_t)bsz * nrhs) * sizeof(T);
+  if (upd_smem > (size_t)ctx->max_smem_optin)
+    return set_error(ctx, LUHOT_ERR_UNSUPPORTED, "getrs: too many right-hand sides for one call");
+  auto uk = trsv_update_kernel<T, kExact, kTrans>;
+  LUHOT_CUDA_TRY(ctx, cudaFuncSetAttribute(uk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)upd_smem));
+  const int nblk = (n + bsz - 1) / bsz;
+  for (int s = 0; s < nblk; ++s) {
+    const int blk = kLower ? s : (nblk - 1 - s);
+    const int j0 = blk * bsz;
+    const int bs = std::min(bsz, n - j0);
+    prof_begin(ctx, kProfTrsv);
+    dk<<<1, 128, (size_t)bs * bs * sizeof(T), stream>>>(a, lda, x, ldx, j0, bs, nrhs);
+    prof_end(ctx, kProfTrsv, (double)bs * bs * nrhs, ((double)bs * bs / 2 + 2.0 * bs * nrhs) * sizeof(T));
+    const int i_begin = kLower ? j0 + bs : 0;
+    const int i_end = kLower ? n : j0;
+    if (i_end > i_begin) {
+      const size_t sm = ((size_t)64 * (bs + 1) + (size_t)bs * nrhs) * sizeof(T);
+      prof_begin(ctx, kProfTrsv);
+      uk<<<(i_end - i_begin + 63) / 64, 256, sm, stream>>>(a, lda, x, ldx, j0, bs, i_begin, i_end, nrhs);
+      const double rows = (double)(i_end - i_begin);
+      prof_end(ctx, kProfTrsv, 2.0 * rows * bs * nrhs,
+               (rows * bs + 2.0 * rows * nrhs + (double)bs * nrhs) * sizeof(T));
+    }
+  }
+  LUHOT_CUDA_TRY(ctx, cudaGetLastError());
+  return LUHOT_OK;
+}
+
+template <typename T>
+int getrs_device(luhot_ctx* ctx, int n, int nrhs, const T* lu, int64_t lda, const int* piv,
+                 const T* b, int64_t ldb, T* x, int64_t ldx, int trans, int mode) {
+  if (n < 0 || nrhs < 0 || lda < std::max(1, n) || ldb < std::max(1, nrhs) || ldx < std::max(1, nrhs))
+    return set_error(ctx, LUHOT_ERR_INVALID_ARG, "getrs: bad shape or leading dimension");
+  if (n == 0 || nrhs == 0) return LUHOT_OK;
+  cudaStream_t stream = ctx->stream;
+  int rc = ensure_buf(ctx, ctx->perm_buf, (size_t)n * sizeof(int));
+  if (rc) return rc;
+  int* perm = static_cast<int*>(ctx->perm_buf.ptr);
+  rc = launch_perm<T>(ctx, piv, n, perm, stream);
+  if (rc) return rc;
+  // Work in a private buffer so that x may alias b.
+  rc = ensure_buf(ctx, ctx->work[3], (size_t)n * nrhs * sizeof(T));
+  if (rc) return rc;
+  T* w = static_cast<T*>(ctx->work[3].ptr);
+  const int64_t ldw = nrhs;
+  const int64_t total = (int64_t)n * nrhs;
+  const int pblocks = (int)((total + 255) / 256);
+  const bool exact = (mode == LUHOT_MODE_EXACT);
+  if (!trans) {
+    prof_begin(ctx, kProfPermute);
+    permute_rows_kernel<T, false><<<pblocks, 256, 0, stream>>>(b, ldb, w, ldw, perm, n, nrhs);
+    prof_end(ctx, kProfPermute, 0.0, 2.0 * total * sizeof(T));
+    if (exact) {
+      rc = blocked_trsv<T, true, true, true, false>(ctx, lu, lda, w, ldw, n, nrhs, stream);
+      if (rc) return rc;
+      const size_t xs = (size_t)n * sizeof(T);
+      const int use_smem = xs <= (size_t)ctx->max_smem_optin - 1024 ? 1 : 0;
+      LUHOT_CUDA_TRY(ctx, cudaFuncSetAttribute(back_exact_kernel<T>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               use_smem ? (int)xs : 0));
+      prof_begin(ctx, kProfTrsv);
+      back_exact_kernel<T><<<nrhs, 32, use_smem ? xs : 0, stream>>>(lu, lda, w, ldw, n, use_smem);
+      prof_end(ctx, kProfTrsv, (double)n * n * nrhs, ((double)n * n / 2 + 2.0 * total) * sizeof(T));
+    } else {
+      rc = blocked_trsv<T, false, true, true, false>(ctx, lu, lda, w, ldw, n, nrhs, stream);
+      if (rc) return rc;
+      rc = blocked_trsv<T, false, false, false, false>(ctx, lu, lda, w, ldw, n, nrhs, stream);
+      if (rc) return rc;
+    }
+    LUHOT_CUDA_TRY(ctx, cudaMemcpy2DAsync(x, ldx * sizeof(T), w, ldw * sizeof(T), nrhs * sizeof(T), n,
+                                          cudaMemcpyDeviceToDevice, stream));
+  } else {
+    // A^T x = b:  U^T z = b (lower, non-unit), L^T y = z (upper, unit), x = P y.
+    LUHOT_CUDA_TRY(ctx, cudaMemcpy2DAsync(w, ldw * sizeof(T), b, ldb * sizeof(T), nrhs * sizeof(T), n,
+                                          cudaMemcpyDeviceToDevice, stream));
+    rc = blocked_trsv<T, false, true, false, true>(ctx, lu, lda, w, ldw, n, nrhs, stream);
+    if (rc) return rc;
+    rc = blocked_trsv<T, false, false, true, true>(ctx, lu, lda, w, ldw, n, nrhs, stream);
+    if (rc) return rc;
+    prof_begin(ctx, kProfPermute);
+    permute_rows_kernel<T, true><<<pblocks, 256, 0, stream>>>(w, ldw, x, ldx, perm, n, nrhs);
+    prof_end(ctx, kProfPermute, 0.0, 2.0 * total * sizeof(T));
+  }
+  LUHOT_CUDA_TRY(ctx, cudaGetLastError());
+  return LUHOT_OK;
+}
+
+template int getrs_device<double>(luhot_ctx*, int, int, const double*, int64_t, const int*,
+                                  const double*, int64_t, double*, int64_t, int, int);
+template int getrs_device<float>(luhot_ctx*, int, int, const float*, int64_t, const int*,
+                                 const float*, int64_t, float*, int64_t, int, int);
+
+}  // namespace luhot

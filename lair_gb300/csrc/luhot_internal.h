@@ -1,0 +1,100 @@
+// Internal declarations shared by the luhot translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <atomic>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "luhot.h"
+
+namespace luhot {
+
+struct DeviceStatus;
+
+constexpr int kMaxPanelCtas = 256;   // >= SM count
+constexpr int kMaxPanelWidth = 64;   // default and largest panel width
+
+// Grow-only device buffer.
+struct DevBuf {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+};
+
+// Kernel classes for the optional CUDA-event profile.
+enum ProfClass : int {
+  kProfPanel = 0,
+  kProfLaswp = 1,
+  kProfTrsm = 2,
+  kProfGemm = 3,
+  kProfTrsv = 4,
+  kProfPermute = 5,
+  kProfRefine = 6,
+  kProfOther = 7,
+  kProfClasses = 8,
+};
+
+struct ProfRecord {
+  int cls;
+  cudaEvent_t start, stop;
+  double flops, bytes;
+};
+
+}  // namespace luhot
+
+struct luhot_ctx {
+  int device = 0;
+  int num_sms = 0;
+  int max_smem_optin = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  std::mutex mu;
+  std::string last_error;
+  luhot::DeviceStatus* d_status = nullptr;
+  luhot::DeviceStatus* h_status = nullptr;  // pinned mirror
+  void* panel_scratch = nullptr;            // candidates of the panel kernel
+  luhot::DevBuf work[4];                    // matrix / rhs / solution / misc
+  luhot::DevBuf piv_buf;                    // int32 pivots
+  luhot::DevBuf perm_buf;                   // int32 permutation
+  void* h_piv = nullptr;                    // pinned pivots staging
+  size_t h_piv_bytes = 0;
+  int nb_override = 0;
+  unsigned long long wait_timeout_ns = 2000000000ull;  // per device-side wait
+  std::atomic<int64_t> launches{0};
+  // CUDA-event profile (off by default): one event pair per launch.
+  bool prof_on = false;
+  std::vector<luhot::ProfRecord> prof_records;
+  std::vector<cudaEvent_t> prof_event_pool;
+  cudaEvent_t prof_pending = nullptr;
+};
+
+namespace luhot {
+
+int set_error(luhot_ctx* ctx, int status, const std::string& msg);
+int reset_status(luhot_ctx* ctx);
+// Synchronises the stream, reads the device status; fills *singular.
+int finish_status(luhot_ctx* ctx, int64_t* singular);
+int ensure_buf(luhot_ctx* ctx, DevBuf& b, size_t bytes);
+
+template <typename T>
+int getrf_device(luhot_ctx* ctx, int m, int n, T* a, int64_t lda, int* piv, int mode,
+                 int64_t* singular);
+
+// Solve with device factors: X (n x nrhs, ldx) <- op(A)^-1 B.  b and x may be
+// the same buffer.
+template <typename T>
+int getrs_device(luhot_ctx* ctx, int n, int nrhs, const T* lu, int64_t lda, const int* piv,
+                 const T* b, int64_t ldb, T* x, int64_t ldx, int trans, int mode);
+
+inline void count_launch(luhot_ctx* ctx, int64_t k = 1) { ctx->launches.fetch_add(k); }
+
+// Bracket one kernel launch: prof_begin records a start event on the
+// context's stream (when profiling), prof_end the stop event plus the
+// launch's algorithmic flops and bytes.  Both count the launch.
+void prof_begin(luhot_ctx* ctx, int cls);
+void prof_end(luhot_ctx* ctx, int cls, double flops, double bytes);
+
+}  // namespace luhot
