@@ -140,6 +140,27 @@ int luhot_dgetrs_dev(luhot_ctx* ctx, int64_t n, int64_t nrhs, const double* d_lu
 int luhot_sgetrs_dev(luhot_ctx* ctx, int64_t n, int64_t nrhs, const float* d_lu, int64_t lda,
                      const int32_t* d_piv, float* d_b, int64_t ldb, int trans, int mode);
 
+/* Scratch held by luhot_dgetrs_dev_noalloc in a static device array. */
+#define LUHOT_NOALLOC_SCRATCH_BYTES (4u << 20)
+
+/* luhot_dgetrs_dev without any allocation: for callers that cannot call
+ * cudaMalloc, such as programs whose device memory is owned by their own pool
+ * or caching allocator, and solve loops that cannot take the device-wide
+ * synchronisation cudaMalloc/cudaFree may cause.  It needs no context (a
+ * context allocates): its scratch is a static device array of
+ * LUHOT_NOALLOC_SCRATCH_BYTES (4 MiB) that every GPU loading this library
+ * keeps until exit.  The caller passes factors, pivots and B (overwritten by
+ * X) in device memory and the stream to run on (NULL = legacy default).
+ * Limit: 4*n rounded up to 256 bytes plus 8*n*nrhs bytes must fit in the
+ * scratch, else LUHOT_ERR_UNSUPPORTED.  The first call on each device looks up
+ * the array's device address (cudaGetSymbolAddress), so make that first call
+ * before any stream capture.  All calls share the array: calls that overlap
+ * on the GPU race on it.  Results equal luhot_dgetrs_dev's.  No counterpart
+ * in lair (lair's getrs allocates its result on the host). */
+int luhot_dgetrs_dev_noalloc(int64_t n, int64_t nrhs, const double* d_lu, int64_t lda,
+                             const int32_t* d_piv, double* d_b, int64_t ldb, int trans, int mode,
+                             void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -55,6 +55,7 @@ SIGNATURES = {
     "luhot_sgetrf_dev": (_i32, [_vp, _i64, _i64, _vp, _i64, _vp, _vp, _i32]),
     "luhot_dgetrs_dev": (_i32, [_vp, _i64, _i64, _vp, _i64, _vp, _vp, _i64, _i32, _i32]),
     "luhot_sgetrs_dev": (_i32, [_vp, _i64, _i64, _vp, _i64, _vp, _vp, _i64, _i32, _i32]),
+    "luhot_dgetrs_dev_noalloc": (_i32, [_i64, _i64, _vp, _i64, _vp, _vp, _i64, _i32, _i32, _vp]),
 }
 
 PROFILE_CLASSES = ("panel", "laswp", "trsm", "gemm", "trsv", "permute", "refine", "other")

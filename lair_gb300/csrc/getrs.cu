@@ -316,4 +316,153 @@ template int getrs_device<double>(luhot_ctx*, int, int, const double*, int64_t, 
 template int getrs_device<float>(luhot_ctx*, int, int, const float*, int64_t, const int*,
                                  const float*, int64_t, float*, int64_t, int, int);
 
+// ---------------------------------------------------------------------------
+// Allocation-free solve (luhot_dgetrs_dev_noalloc).
+//
+// Some callers cannot call cudaMalloc: a host program whose device memory is
+// all owned by its own pool or caching allocator (a raw cudaMalloc there
+// either fails because the pool reserved the memory up front, or escapes the
+// pool's accounting), and latency-critical solve loops where the implicit
+// device-wide synchronisation of cudaMalloc/cudaFree is not acceptable.  A
+// luhot context allocates its workspace, so this path needs no context: the
+// scratch it needs (the row permutation and a copy of the right-hand sides)
+// lives in the file-scope array below, which every GPU that loads this
+// library holds until the process exits.  Every call uses the same array;
+// calls that overlap on the GPU (different streams, or other host threads)
+// race on it.  Each call writes every scratch byte it reads first (the
+// permutation kernel fills all n entries, the gather all n x nrhs values), so
+// nothing in it needs clearing between calls.
+// ---------------------------------------------------------------------------
+constexpr size_t kNoAllocScratchBytes = (size_t)LUHOT_NOALLOC_SCRATCH_BYTES;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+namespace {
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[kNoAllocMaxDevices] = {};  // device address of g_noalloc_scratch, per device
+int g_noalloc_smem[kNoAllocMaxDevices] = {};
+
+// Once per device, with that device current: look up the device address of
+// the scratch array.  In host code `g_noalloc_scratch` names a host-side
+// stand-in, never the device memory, so kernels only ever get this address.
+int noalloc_setup(void** scratch, int* max_smem) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return LUHOT_ERR_CUDA;
+  }
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return LUHOT_ERR_UNSUPPORTED;
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress((void**)&p, g_noalloc_scratch) != cudaSuccess || !p) {
+      cudaGetLastError();
+      return LUHOT_ERR_CUDA;
+    }
+    int smem = 0;
+    if (cudaDeviceGetAttribute(&smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+      cudaGetLastError();
+      return LUHOT_ERR_CUDA;
+    }
+    g_noalloc_smem[dev] = smem;
+    g_noalloc_addr[dev] = p;
+  }
+  *scratch = g_noalloc_addr[dev];
+  *max_smem = g_noalloc_smem[dev];
+  return LUHOT_OK;
+}
+
+template <typename T, bool kExact, bool kLower, bool kUnit, bool kTrans>
+cudaError_t trsv_noalloc(const T* a, int64_t lda, T* x, int64_t ldx, int n, int nrhs, cudaStream_t stream) {
+  const int bsz = kTrsvBlock;
+  auto dk = trsv_diag_kernel<T, kExact, kLower, kUnit, kTrans>;
+  auto uk = trsv_update_kernel<T, kExact, kTrans>;
+  cudaError_t e = cudaFuncSetAttribute(dk, cudaFuncAttributeMaxDynamicSharedMemorySize, bsz * bsz * (int)sizeof(T));
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(uk, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)(((size_t)64 * (bsz + 1) + (size_t)bsz * nrhs) * sizeof(T)));
+  if (e != cudaSuccess) return e;
+  const int nblk = (n + bsz - 1) / bsz;
+  for (int s = 0; s < nblk; ++s) {
+    const int blk = kLower ? s : (nblk - 1 - s);
+    const int j0 = blk * bsz;
+    const int bs = std::min(bsz, n - j0);
+    dk<<<1, 128, (size_t)bs * bs * sizeof(T), stream>>>(a, lda, x, ldx, j0, bs, nrhs);
+    const int i_begin = kLower ? j0 + bs : 0;
+    const int i_end = kLower ? n : j0;
+    if (i_end > i_begin) {
+      const size_t sm = ((size_t)64 * (bs + 1) + (size_t)bs * nrhs) * sizeof(T);
+      uk<<<(i_end - i_begin + 63) / 64, 256, sm, stream>>>(a, lda, x, ldx, j0, bs, i_begin, i_end, nrhs);
+    }
+  }
+  return cudaGetLastError();
+}
+}  // namespace
+
 }  // namespace luhot
+
+extern "C" int luhot_dgetrs_dev_noalloc(int64_t n, int64_t nrhs, const double* d_lu, int64_t lda,
+                                        const int32_t* d_piv, double* d_b, int64_t ldb, int trans,
+                                        int mode, void* cuda_stream) {
+  using namespace luhot;
+  if (n < 0 || nrhs < 0 || n >= INT32_MAX || nrhs >= INT32_MAX) return LUHOT_ERR_INVALID_ARG;
+  if (mode != LUHOT_MODE_FAST && mode != LUHOT_MODE_EXACT) return LUHOT_ERR_INVALID_ARG;
+  if (n == 0 || nrhs == 0) return LUHOT_OK;
+  if (!d_lu || !d_piv || !d_b || lda < n || ldb < nrhs) return LUHOT_ERR_INVALID_ARG;
+  const size_t perm_bytes = ((size_t)n * sizeof(int) + 255) / 256 * 256;
+  const size_t work_bytes = (size_t)n * (size_t)nrhs * sizeof(double);
+  if (perm_bytes + work_bytes > kNoAllocScratchBytes) return LUHOT_ERR_UNSUPPORTED;
+  void* scratch = nullptr;
+  int max_smem = 0;
+  int rc = noalloc_setup(&scratch, &max_smem);
+  if (rc) return rc;
+  if (((size_t)64 * (kTrsvBlock + 1) + (size_t)kTrsvBlock * nrhs) * sizeof(double) > (size_t)max_smem)
+    return LUHOT_ERR_UNSUPPORTED;
+  cudaStream_t stream = static_cast<cudaStream_t>(cuda_stream);
+  int* perm = static_cast<int*>(scratch);
+  double* w = reinterpret_cast<double*>(static_cast<unsigned char*>(scratch) + perm_bytes);
+  const int nn = (int)n, nr = (int)nrhs;
+  const int64_t ldw = nrhs;
+  const int64_t total = n * nrhs;
+  const int pblocks = (int)((total + 255) / 256);
+  const int use_smem = 2 * (size_t)n * sizeof(int) <= (size_t)max_smem ? 1 : 0;
+  if (cudaFuncSetAttribute(perm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           use_smem ? (int)(2 * n * sizeof(int)) : 0) != cudaSuccess) {
+    cudaGetLastError();
+    return LUHOT_ERR_CUDA;
+  }
+  perm_kernel<<<1, 1024, use_smem ? 2 * n * sizeof(int) : 0, stream>>>(d_piv, nn, perm, use_smem);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess && !trans) {
+    permute_rows_kernel<double, false><<<pblocks, 256, 0, stream>>>(d_b, ldb, w, ldw, perm, nn, nr);
+    if (mode == LUHOT_MODE_EXACT) {
+      e = trsv_noalloc<double, true, true, true, false>(d_lu, lda, w, ldw, nn, nr, stream);
+      const size_t xs = (size_t)n * sizeof(double);
+      const int xs_smem = xs <= (size_t)max_smem - 1024 ? 1 : 0;
+      if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(back_exact_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 xs_smem ? (int)xs : 0);
+      if (e == cudaSuccess)
+        back_exact_kernel<double><<<nr, 32, xs_smem ? xs : 0, stream>>>(d_lu, lda, w, ldw, nn, xs_smem);
+    } else {
+      e = trsv_noalloc<double, false, true, true, false>(d_lu, lda, w, ldw, nn, nr, stream);
+      if (e == cudaSuccess) e = trsv_noalloc<double, false, false, false, false>(d_lu, lda, w, ldw, nn, nr, stream);
+    }
+    if (e == cudaSuccess)
+      e = cudaMemcpy2DAsync(d_b, ldb * sizeof(double), w, ldw * sizeof(double), nrhs * sizeof(double), n,
+                            cudaMemcpyDeviceToDevice, stream);
+  } else if (e == cudaSuccess) {
+    e = cudaMemcpy2DAsync(w, ldw * sizeof(double), d_b, ldb * sizeof(double), nrhs * sizeof(double), n,
+                          cudaMemcpyDeviceToDevice, stream);
+    if (e == cudaSuccess) e = trsv_noalloc<double, false, true, false, true>(d_lu, lda, w, ldw, nn, nr, stream);
+    if (e == cudaSuccess) e = trsv_noalloc<double, false, false, true, true>(d_lu, lda, w, ldw, nn, nr, stream);
+    if (e == cudaSuccess)
+      permute_rows_kernel<double, true><<<pblocks, 256, 0, stream>>>(w, ldw, d_b, ldb, perm, nn, nr);
+  }
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return LUHOT_ERR_CUDA;
+  }
+  return LUHOT_OK;
+}
