@@ -323,6 +323,12 @@ def run_ours(args):
                "ms_per_step": dt / args.steps * 1e3}
         _lib.check(lib.luhot_set_stream(ctx, ctypes.c_void_p(stream.cuda_stream)), ctx)
 
+    ir = None
+    if not args.no_ir:
+        del A, A0, X
+        torch.cuda.empty_cache()
+        ir = run_ir(args, lib, ctx, torch, rank)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_baseline(n, args.cpu_seconds)
@@ -334,10 +340,89 @@ def run_ours(args):
                 "config": workload_config(args), "backward_error": berr, "berr_bound": n * EPS64,
                 "berr_ok": berr <= n * EPS64, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                 "clocks": clocks.summary(), "gpu_launches": int(launches),
-                "kernel_profile_ms": {k: round(v["ms"], 3) for k, v in prof.items()}}
+                "kernel_profile_ms": {k: round(v["ms"], 3) for k, v in prof.items()}, "ir": ir}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def conditioned_system(n, kappa, seed, torch):
+    """A = Q1 diag(sigma) Q2^T, Q from Householder QR of seeded N(0,1) matrices
+    (FP32 QR on the GPU: the orthogonality error ~1e-6 perturbs the singular
+    values only relatively, so kappa is kept), sigma geometric 1 -> 1/kappa,
+    product formed in FP64; b iid N(0,1)."""
+    gen = torch.Generator(device="cuda").manual_seed(seed)
+    q1, _ = torch.linalg.qr(torch.randn((n, n), device="cuda", generator=gen))
+    q2, _ = torch.linalg.qr(torch.randn((n, n), device="cuda", generator=gen))
+    sigma = torch.logspace(0, -float(np.log10(kappa)), n, dtype=torch.float64, device="cuda")
+    a = (q1.double() * sigma) @ q2.double().T
+    del q1, q2
+    b = torch.randn(n, dtype=torch.float64, device="cuda", generator=gen)
+    return a.contiguous(), b
+
+
+def run_ir(args, lib, ctx, torch, rank):
+    """Mixed-precision LU + refinement on the kappa-conditioned n x n system,
+    against the plain FP64 LU on the same system."""
+    import ctypes
+
+    from lair_gb300 import _lib
+
+    n = args.ir_n
+    kappa = args.ir_kappa
+    t0 = time.perf_counter()
+    A, b = conditioned_system(n, kappa, 7 + rank, torch)
+    torch.cuda.synchronize()
+    gen_s = time.perf_counter() - t0
+    x = torch.empty_like(b)
+    stream = torch.cuda.current_stream()
+    results = {}
+    for solver in ("ir", "gmres"):
+        info = _lib.IrInfo()
+
+        def solve():
+            rc = lib.luhot_dgesv_ir_dev(ctx, n, 1, A.data_ptr(), n, b.data_ptr(), 1, x.data_ptr(), 1,
+                                        _lib.PREC_FP32, _lib.SOLVERS[solver], 0.0, 50, ctypes.byref(info))
+            _lib.check(rc, ctx)
+
+        reps = args.steps if solver == "ir" else 1
+        for _ in range(args.warmup if solver == "ir" else 1):
+            solve()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            solve()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        R = b - A @ x
+        berr = (R.abs().max() / (A.abs().sum(1).max() * x.abs().max() + b.abs().max())).item()
+        results[solver] = {"ms": ms, "gflops": flops_of(n, 1) / (ms * 1e-3) / 1e9, "iterations": info.iterations,
+                           "inner_iterations": info.inner_iterations, "backward_error": berr,
+                           "berr_ok": berr <= n * EPS64, "factor_ms": info.factor_ms, "refine_ms": info.refine_ms}
+    # plain FP64 LU on the same system, once
+    Aw = A.clone()
+    piv = torch.empty(n, dtype=torch.int32, device="cuda")
+    xf = b.clone().reshape(n, 1)
+    sing = ctypes.c_int64(0)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    _lib.check(lib.luhot_dgetrf_dev(ctx, n, n, Aw.data_ptr(), n, piv.data_ptr(), ctypes.byref(sing), 0), ctx)
+    _lib.check(lib.luhot_dgetrs_dev(ctx, n, 1, Aw.data_ptr(), n, piv.data_ptr(), xf.data_ptr(), 1, 0, 0), ctx)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    fp64_ms = e0.elapsed_time(e1)
+    R = b - A @ xf[:, 0]
+    fp64_berr = (R.abs().max() / (A.abs().sum(1).max() * xf.abs().max() + b.abs().max())).item()
+    best = min(results, key=lambda k: results[k]["ms"] if results[k]["berr_ok"] else float("inf"))
+    return {"workload": f"kappa={kappa:g} system, n={n}, nrhs=1, A=Q1 diag(sigma) Q2^T, b iid N(0,1)",
+            "precision": "fp32 factorization (FFMA), fp64 residual/update", "n": n, "kappa": kappa,
+            "generation_s": gen_s, "plain_ir": results["ir"], "gmres_ir": results["gmres"],
+            "fp64_lu_ms": fp64_ms, "fp64_lu_gflops": flops_of(n, 1) / (fp64_ms * 1e-3) / 1e9,
+            "fp64_backward_error": fp64_berr, "best": best,
+            "speedup_vs_fp64": fp64_ms / results[best]["ms"], "berr_bound": n * EPS64}
 
 
 def main():
@@ -354,6 +439,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-elim-steps", type=int, default=4)
+    ap.add_argument("--no-ir", action="store_true")
+    ap.add_argument("--ir-n", type=int, default=16384)
+    ap.add_argument("--ir-kappa", type=float, default=1e6)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

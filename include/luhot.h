@@ -124,6 +124,46 @@ int luhot_dgesv(luhot_ctx* ctx, int64_t n, int64_t nrhs, const double* a, int64_
                 int64_t cs, const double* b, int64_t b_rs, int64_t b_cs, double* x, int64_t x_rs,
                 int64_t x_cs, int mode);
 
+/* ---- Mixed-precision LU with iterative refinement ---------------------
+ * No lair counterpart: an alternative to luhot_dgesv for square FP64
+ * systems.  A is factored in a low precision; FP64 is used only for the
+ * residual r = b - A x, the update x += d and the stopping test on the
+ * normwise backward error ||r||_inf / (||A||_inf ||x||_inf + ||b||_inf) <= tol
+ * (tol <= 0 selects n * 2^-53, lair's Real::eps for f64 times n).
+ * LUHOT_REFINE_IR: d = (LU)^-1 r in the low precision (converges for
+ * kappa * u_low < 1); LUHOT_REFINE_GMRES: d from FP64 GMRES preconditioned
+ * by the low-precision LU (Carson & Higham), for larger kappa * u_low. */
+#define LUHOT_PREC_FP32 0
+#define LUHOT_PREC_BF16 1
+#define LUHOT_PREC_FP16 2
+#define LUHOT_REFINE_IR 0
+#define LUHOT_REFINE_GMRES 1
+
+typedef struct luhot_ir_info {
+  int iterations;         /* refinement steps (max over right-hand sides) */
+  int inner_iterations;   /* GMRES iterations, summed (0 for plain IR) */
+  int converged;          /* 1 when every column reached tol */
+  int precision;          /* LUHOT_PREC_* used for the factorization */
+  int solver;             /* LUHOT_REFINE_* */
+  double backward_error;  /* final normwise backward error (max over columns) */
+  double factor_ms;       /* conversion + low-precision LU (CUDA events) */
+  double refine_ms;       /* everything after the factorization */
+  int64_t singular;       /* singular step of the low-precision LU, -1 none */
+} luhot_ir_info;
+
+/* Device-resident: A (n x n, lda) and B (n x nrhs, ldb) row-major FP64 in HBM
+ * are not modified; X (n x nrhs, ldx) receives the solution.  Returns
+ * LUHOT_ERR_NOT_CONVERGED (X holds the last iterate) when tol is not reached
+ * within max_iter steps or the iteration stops contracting, and
+ * LUHOT_ERR_SINGULAR when the low-precision factor is singular. */
+int luhot_dgesv_ir_dev(luhot_ctx* ctx, int64_t n, int64_t nrhs, const double* d_a, int64_t lda,
+                       const double* d_b, int64_t ldb, double* d_x, int64_t ldx, int precision,
+                       int solver, double tol, int max_iter, luhot_ir_info* info);
+/* Host-buffer form of luhot_dgesv_ir_dev (any strides). */
+int luhot_dgesv_ir(luhot_ctx* ctx, int64_t n, int64_t nrhs, const double* a, int64_t rs, int64_t cs,
+                   const double* b, int64_t b_rs, int64_t b_cs, double* x, int64_t x_rs, int64_t x_cs,
+                   int precision, int solver, double tol, int max_iter, luhot_ir_info* info);
+
 /* ---- Device-resident entry points ------------------------------------ */
 /* Matrices are row-major on the device with leading dimension ld (elements);
  * pivots are int32 on the device.  The call is asynchronous on the context's

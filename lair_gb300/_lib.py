@@ -55,6 +55,9 @@ SIGNATURES = {
     "luhot_sgetrf_dev": (_i32, [_vp, _i64, _i64, _vp, _i64, _vp, _vp, _i32]),
     "luhot_dgetrs_dev": (_i32, [_vp, _i64, _i64, _vp, _i64, _vp, _vp, _i64, _i32, _i32]),
     "luhot_sgetrs_dev": (_i32, [_vp, _i64, _i64, _vp, _i64, _vp, _vp, _i64, _i32, _i32]),
+    "luhot_dgesv_ir_dev": (_i32, [_vp, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _i32, _i32, _dbl, _i32, _vp]),
+    "luhot_dgesv_ir": (_i32, [_vp, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _i32, _i32, _dbl,
+                              _i32, _vp]),
     "luhot_dgetrs_dev_noalloc": (_i32, [_i64, _i64, _vp, _i64, _vp, _vp, _i64, _i32, _i32, _vp]),
 }
 
@@ -69,6 +72,22 @@ class Profile(ctypes.Structure):
         return {name: {"ms": self.ms[i], "flops": self.flops[i], "bytes": self.bytes[i],
                        "launches": int(self.launches[i])}
                 for i, name in enumerate(PROFILE_CLASSES) if self.launches[i]}
+
+
+PREC_FP32, PREC_BF16, PREC_FP16 = 0, 1, 2
+PRECISIONS = {"fp32": PREC_FP32, "bf16": PREC_BF16, "fp16": PREC_FP16}
+REFINE_IR, REFINE_GMRES = 0, 1
+SOLVERS = {"ir": REFINE_IR, "gmres": REFINE_GMRES}
+
+
+class IrInfo(ctypes.Structure):
+    """luhot_ir_info"""
+    _fields_ = [("iterations", _i32), ("inner_iterations", _i32), ("converged", _i32), ("precision", _i32),
+                ("solver", _i32), ("backward_error", _dbl), ("factor_ms", _dbl), ("refine_ms", _dbl),
+                ("singular", _i64)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
 
 
 _lib = None

@@ -96,6 +96,37 @@ static int launch_transpose(luhot_ctx* ctx, const T* src, int64_t lds, T* dst, i
 
 static int64_t round_up(int64_t v, int64_t m) { return (v + m - 1) / m * m; }
 
+// Strided device-to-device copy of `rows` rows of `wbytes` bytes (4-byte units).
+__global__ void copy_rows_kernel(unsigned char* dst, size_t dpitch, const unsigned char* src, size_t spitch,
+                                 size_t words, size_t rows) {
+  const size_t total = words * rows;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = t / words, w = t - r * words;
+    reinterpret_cast<uint32_t*>(dst + r * dpitch)[w] = reinterpret_cast<const uint32_t*>(src + r * spitch)[w];
+  }
+}
+
+int copy_2d(luhot_ctx* ctx, void* dst, size_t dpitch, const void* src, size_t spitch, size_t wbytes, size_t rows,
+            cudaMemcpyKind kind) {
+  if (wbytes == 0 || rows == 0) return LUHOT_OK;
+  if ((dpitch == wbytes && spitch == wbytes) || rows == 1) {
+    LUHOT_CUDA_TRY(ctx, cudaMemcpyAsync(dst, src, wbytes * rows, kind, ctx->stream));
+    return LUHOT_OK;
+  }
+  if (kind == cudaMemcpyDeviceToDevice && wbytes % 4 == 0 && dpitch % 4 == 0 && spitch % 4 == 0 &&
+      (reinterpret_cast<uintptr_t>(dst) & 3) == 0 && (reinterpret_cast<uintptr_t>(src) & 3) == 0) {
+    const size_t total = wbytes / 4 * rows;
+    const int blocks = (int)std::min<size_t>((total + 255) / 256, (size_t)ctx->num_sms * 8);
+    copy_rows_kernel<<<blocks, 256, 0, ctx->stream>>>(static_cast<unsigned char*>(dst), dpitch,
+                                                      static_cast<const unsigned char*>(src), spitch, wbytes / 4, rows);
+    count_launch(ctx);
+    LUHOT_CUDA_TRY(ctx, cudaGetLastError());
+    return LUHOT_OK;
+  }
+  LUHOT_CUDA_TRY(ctx, cudaMemcpy2DAsync(dst, dpitch, src, spitch, wbytes, rows, kind, ctx->stream));
+  return LUHOT_OK;
+}
+
 // Two co-resident CTAs wait for three arrivals: the wait can only end by its
 // time limit.  Exercises the timeout path of grid_barrier without a fault.
 __global__ void unreachable_barrier_kernel(DeviceStatus* st) {
@@ -130,8 +161,11 @@ static int stage_in(luhot_ctx* ctx, const T* h, int64_t m, int64_t n, int64_t rs
   const Layout lay = classify(m, n, rs, cs);
   if (lay == Layout::kC) {
     const int64_t src_ld = (m <= 1) ? n : rs;
-    LUHOT_CUDA_TRY(ctx, cudaMemcpy2DAsync(d, ldd * sizeof(T), h, src_ld * sizeof(T), n * sizeof(T), m,
-                                          cudaMemcpyHostToDevice, ctx->stream));
+    {
+      int rc_ = copy_2d(ctx, d, ldd * sizeof(T), h, src_ld * sizeof(T), n * sizeof(T), m,
+                                          cudaMemcpyHostToDevice);
+      if (rc_) return rc_;
+    }
     return LUHOT_OK;
   }
   if (lay == Layout::kF) {
@@ -139,15 +173,21 @@ static int stage_in(luhot_ctx* ctx, const T* h, int64_t m, int64_t n, int64_t rs
     int rc = ensure_buf(ctx, tmp, (size_t)m * n * sizeof(T));
     if (rc) return rc;
     T* t = static_cast<T*>(tmp.ptr);  // n x m row-major (= A^T)
-    LUHOT_CUDA_TRY(ctx, cudaMemcpy2DAsync(t, m * sizeof(T), h, src_ld * sizeof(T), m * sizeof(T), n,
-                                          cudaMemcpyHostToDevice, ctx->stream));
+    {
+      int rc_ = copy_2d(ctx, t, m * sizeof(T), h, src_ld * sizeof(T), m * sizeof(T), n,
+                                          cudaMemcpyHostToDevice);
+      if (rc_) return rc_;
+    }
     return launch_transpose<T>(ctx, t, m, d, ldd, (int)n, (int)m);
   }
   std::vector<T> packed((size_t)m * n);
   for (int64_t i = 0; i < m; ++i)
     for (int64_t j = 0; j < n; ++j) packed[(size_t)i * n + j] = h[i * rs + j * cs];
-  LUHOT_CUDA_TRY(ctx, cudaMemcpy2DAsync(d, ldd * sizeof(T), packed.data(), n * sizeof(T), n * sizeof(T), m,
-                                        cudaMemcpyHostToDevice, ctx->stream));
+  {
+      int rc_ = copy_2d(ctx, d, ldd * sizeof(T), packed.data(), n * sizeof(T), n * sizeof(T), m,
+                                        cudaMemcpyHostToDevice);
+      if (rc_) return rc_;
+    }
   LUHOT_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));  // packed goes out of scope
   return LUHOT_OK;
 }
@@ -160,8 +200,11 @@ static int stage_out(luhot_ctx* ctx, const T* d, int64_t ldd, T* h, int64_t m, i
   const Layout lay = classify(m, n, rs, cs);
   if (lay == Layout::kC) {
     const int64_t dst_ld = (m <= 1) ? n : rs;
-    LUHOT_CUDA_TRY(ctx, cudaMemcpy2DAsync(h, dst_ld * sizeof(T), d, ldd * sizeof(T), n * sizeof(T), m,
-                                          cudaMemcpyDeviceToHost, ctx->stream));
+    {
+      int rc_ = copy_2d(ctx, h, dst_ld * sizeof(T), d, ldd * sizeof(T), n * sizeof(T), m,
+                                          cudaMemcpyDeviceToHost);
+      if (rc_) return rc_;
+    }
     LUHOT_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     return LUHOT_OK;
   }
@@ -172,14 +215,20 @@ static int stage_out(luhot_ctx* ctx, const T* d, int64_t ldd, T* h, int64_t m, i
     T* t = static_cast<T*>(tmp.ptr);
     rc = launch_transpose<T>(ctx, d, ldd, t, m, (int)m, (int)n);
     if (rc) return rc;
-    LUHOT_CUDA_TRY(ctx, cudaMemcpy2DAsync(h, dst_ld * sizeof(T), t, m * sizeof(T), m * sizeof(T), n,
-                                          cudaMemcpyDeviceToHost, ctx->stream));
+    {
+      int rc_ = copy_2d(ctx, h, dst_ld * sizeof(T), t, m * sizeof(T), m * sizeof(T), n,
+                                          cudaMemcpyDeviceToHost);
+      if (rc_) return rc_;
+    }
     LUHOT_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     return LUHOT_OK;
   }
   std::vector<T> packed((size_t)m * n);
-  LUHOT_CUDA_TRY(ctx, cudaMemcpy2DAsync(packed.data(), n * sizeof(T), d, ldd * sizeof(T), n * sizeof(T), m,
-                                        cudaMemcpyDeviceToHost, ctx->stream));
+  {
+      int rc_ = copy_2d(ctx, packed.data(), n * sizeof(T), d, ldd * sizeof(T), n * sizeof(T), m,
+                                        cudaMemcpyDeviceToHost);
+      if (rc_) return rc_;
+    }
   LUHOT_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   for (int64_t i = 0; i < m; ++i)
     for (int64_t j = 0; j < n; ++j) h[i * rs + j * cs] = packed[(size_t)i * n + j];
@@ -319,6 +368,7 @@ int luhot_create(luhot_ctx** out, int device) {
   ctx->stream = ctx->own_stream;
   ok = ok && cudaMalloc(&ctx->d_status, sizeof(DeviceStatus)) == cudaSuccess;
   ok = ok && cudaMallocHost(&ctx->h_status, sizeof(DeviceStatus)) == cudaSuccess;
+  ok = ok && cudaMallocHost(&ctx->h_scalars, 256 * sizeof(double)) == cudaSuccess;
   const size_t scratch = (2 * (size_t)kMaxPanelCtas + 2 * (size_t)kMaxPanelCtas * kMaxPanelWidth +
                           2 * (size_t)kMaxPanelWidth) * sizeof(double) +
                          2 * (size_t)kMaxPanelCtas * sizeof(int);
@@ -340,9 +390,13 @@ void luhot_destroy(luhot_ctx* ctx) {
     if (b.ptr) cudaFree(b.ptr);
   if (ctx->piv_buf.ptr) cudaFree(ctx->piv_buf.ptr);
   if (ctx->perm_buf.ptr) cudaFree(ctx->perm_buf.ptr);
+  if (ctx->trsv_buf.ptr) cudaFree(ctx->trsv_buf.ptr);
   if (ctx->panel_scratch) cudaFree(ctx->panel_scratch);
   if (ctx->d_status) cudaFree(ctx->d_status);
   if (ctx->h_status) cudaFreeHost(ctx->h_status);
+  if (ctx->h_scalars) cudaFreeHost(ctx->h_scalars);
+  for (auto& b : ctx->ir_buf)
+    if (b.ptr) cudaFree(b.ptr);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
 }
@@ -474,6 +528,50 @@ int luhot_sgetrs_dev(luhot_ctx* ctx, int64_t n, int64_t nrhs, const float* d_lu,
   if (!dims_ok(n, nrhs)) return set_error(ctx, LUHOT_ERR_INVALID_ARG, "getrs: invalid dimensions");
   if (n > 0 && nrhs > 0 && (!d_lu || !d_piv || !d_b)) return set_error(ctx, LUHOT_ERR_INVALID_ARG, "getrs: null pointer");
   return getrs_device<float>(ctx, (int)n, (int)nrhs, d_lu, lda, d_piv, d_b, ldb, d_b, ldb, trans, mode);
+}
+
+int luhot_dgesv_ir_dev(luhot_ctx* ctx, int64_t n, int64_t nrhs, const double* d_a, int64_t lda,
+                       const double* d_b, int64_t ldb, double* d_x, int64_t ldx, int precision, int solver,
+                       double tol, int max_iter, luhot_ir_info* info) {
+  if (!ctx || !info) return LUHOT_ERR_INVALID_ARG;
+  Guard g(ctx);
+  if (!dims_ok(n, nrhs) || !dims_ok(n, n)) return set_error(ctx, LUHOT_ERR_INVALID_ARG, "gesv_ir: invalid dimensions");
+  if (n > 0 && nrhs > 0 && (!d_a || !d_b || !d_x)) return set_error(ctx, LUHOT_ERR_INVALID_ARG, "gesv_ir: null pointer");
+  return gesv_ir_device(ctx, (int)n, (int)nrhs, d_a, lda, d_b, ldb, d_x, ldx, precision, solver, tol, max_iter, info);
+}
+
+int luhot_dgesv_ir(luhot_ctx* ctx, int64_t n, int64_t nrhs, const double* a, int64_t rs, int64_t cs,
+                   const double* b, int64_t b_rs, int64_t b_cs, double* x, int64_t x_rs, int64_t x_cs, int precision,
+                   int solver, double tol, int max_iter, luhot_ir_info* info) {
+  if (!ctx || !info) return LUHOT_ERR_INVALID_ARG;
+  Guard g(ctx);
+  if (!dims_ok(n, nrhs) || !dims_ok(n, n)) return set_error(ctx, LUHOT_ERR_INVALID_ARG, "gesv_ir: invalid dimensions");
+  if (n == 0 || nrhs == 0) {
+    *info = luhot_ir_info{};
+    info->converged = 1;
+    info->singular = -1;
+    return LUHOT_OK;
+  }
+  if (!a || !b || !x) return set_error(ctx, LUHOT_ERR_INVALID_ARG, "gesv_ir: null pointer");
+  const int64_t lda = dev_ld<double>(n);
+  int rc = ensure_buf(ctx, ctx->work[0], (size_t)n * lda * sizeof(double));
+  if (rc) return rc;
+  rc = ensure_buf(ctx, ctx->work[2], (size_t)n * nrhs * 2 * sizeof(double));
+  if (rc) return rc;
+  double* d_a = static_cast<double*>(ctx->work[0].ptr);
+  double* d_b = static_cast<double*>(ctx->work[2].ptr);
+  double* d_x = d_b + (size_t)n * nrhs;
+  rc = stage_in<double>(ctx, a, n, n, rs, cs, d_a, lda, ctx->work[1]);
+  if (rc) return rc;
+  rc = stage_in<double>(ctx, b, n, nrhs, b_rs, b_cs, d_b, nrhs, ctx->work[1]);
+  if (rc) return rc;
+  rc = gesv_ir_device(ctx, (int)n, (int)nrhs, d_a, lda, d_b, nrhs, d_x, nrhs, precision, solver, tol, max_iter, info);
+  if (rc != LUHOT_OK && rc != LUHOT_ERR_NOT_CONVERGED) return rc;
+  const std::string msg = ctx->last_error;
+  const int rc2 = stage_out<double>(ctx, d_x, nrhs, x, n, nrhs, x_rs, x_cs, ctx->work[1]);
+  if (rc2) return rc2;
+  if (rc) ctx->last_error = msg;
+  return rc;
 }
 
 }  // extern "C"

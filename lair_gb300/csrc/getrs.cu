@@ -9,20 +9,24 @@
 // P^T b is one gather through the permutation that the interchanges compose
 // to (computed once by perm_kernel); P w is the matching scatter.
 //
-// Blocked triangular solves: a diagonal-block kernel (one CTA, sequential per
-// right-hand side) and an update kernel for the rows outside the block (one
-// thread per (row, rhs), the block of A staged in shared memory).
-// In exact mode the forward sweep keeps lair's order (each row subtracts
-// l[i][k] * x[k] for increasing k, multiply and subtract rounded apart).  The
-// backward sweep in lair subtracts u[i][k] * x[k] for k = i+1 .. n-1 in
-// increasing k, which makes every row wait for the row below it and the
-// whole sweep one dependent chain of n^2/2 subtractions; exact mode runs that
-// chain literally (back_exact_kernel, one warp per right-hand side).  Fast
-// mode blocks the backward sweep too and uses FMA.
+// Triangular sweeps run as one sync-free launch each (trsv.cu).  In exact mode
+// the forward sweep keeps lair's order (each row subtracts l[i][k] * x[k] for
+// increasing k, multiply and subtract rounded apart).  The backward sweep in
+// lair subtracts u[i][k] * x[k] for k = i+1 .. n-1 in increasing k, which
+// makes every row wait for the row below it and the whole sweep one dependent
+// chain of n^2/2 subtractions; exact mode runs that chain literally
+// (back_exact_kernel, one warp per right-hand side).  Fast mode sweeps both
+// triangles sync-free with FMA.
+//
+// The allocation-free entry point at the end of this file uses the simpler
+// blocked kernels below (a diagonal-block kernel, sequential per right-hand
+// side, and an update kernel for the rows outside the block), which need no
+// scratch besides the permutation and the right-hand-side copy.
 #include <algorithm>
 
 #include "common.cuh"
 #include "luhot_internal.h"
+#include "trsv.cuh"
 
 namespace luhot {
 
@@ -203,50 +207,87 @@ __global__ void back_exact_kernel(const T* u, int64_t lda, T* x, int64_t ldx, in
   }
 }
 
-template <typename T>
-static int launch_perm(luhot_ctx* ctx, const int* piv, int n, int* perm, cudaStream_t stream) {
+int getrs_perm(luhot_ctx* ctx, const int* piv, int n, int* perm) {
   const size_t bytes = 2 * (size_t)n * sizeof(int);  // permutation + pivots
   const int use_smem = bytes <= (size_t)ctx->max_smem_optin ? 1 : 0;
   const size_t smem = use_smem ? bytes : 0;
-  LUHOT_CUDA_TRY(ctx, cudaFuncSetAttribute(perm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)std::max<size_t>(smem, 0)));
+  LUHOT_CUDA_TRY(ctx, cudaFuncSetAttribute(perm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   prof_begin(ctx, kProfPermute);
-  perm_kernel<<<1, 1024, smem, stream>>>(piv, n, perm, use_smem);
+  perm_kernel<<<1, 1024, smem, ctx->stream>>>(piv, n, perm, use_smem);
   prof_end(ctx, kProfPermute, 0.0, 2.0 * n * sizeof(int));
   LUHOT_CUDA_TRY(ctx, cudaGetLastError());
   return LUHOT_OK;
 }
 
-template <typename T, bool kExact, bool kLower, bool kUnit, bool kTrans>
-static int blocked_trsv(luhot_ctx* ctx, const T* a, int64_t lda, T* x, int64_t ldx, int n, int nrhs,
-                        cudaStream_t stream) {
-  const int bsz = kTrsvBlock;
-  const size_t diag_smem = (size_t)bsz * bsz * sizeof(T);
-  auto dk = trsv_diag_kernel<T, kExact, kLower, kUnit, kTrans>;
-  LUHOT_CUDA_TRY(ctx, cudaFuncSetAttribute(dk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)diag_smem));
-  const size_t upd_smem = ((size_t)64 * (bsz + 1) + (size_t)bsz * nrhs) * sizeof(T);
-  if (upd_smem > (size_t)ctx->max_smem_optin)
-    return set_error(ctx, LUHOT_ERR_UNSUPPORTED, "getrs: too many right-hand sides for one call");
-  auto uk = trsv_update_kernel<T, kExact, kTrans>;
-  LUHOT_CUDA_TRY(ctx, cudaFuncSetAttribute(uk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)upd_smem));
-  const int nblk = (n + bsz - 1) / bsz;
-  for (int s = 0; s < nblk; ++s) {
-    const int blk = kLower ? s : (nblk - 1 - s);
-    const int j0 = blk * bsz;
-    const int bs = std::min(bsz, n - j0);
+int trsv_scratch(luhot_ctx* ctx, int n, int** flags, int** ticket) {
+  const int nblk = trsv_syncfree_blocks(n);
+  int rc = ensure_buf(ctx, ctx->trsv_buf, ((size_t)nblk + 64) * sizeof(int));
+  if (rc) return rc;
+  *flags = static_cast<int*>(ctx->trsv_buf.ptr);
+  *ticket = *flags + ((nblk + 31) / 32) * 32;
+  return LUHOT_OK;
+}
+
+template <typename T>
+int getrs_apply(luhot_ctx* ctx, int n, int nrhs, const T* lu, int64_t lda, const int* perm, const T* b,
+                int64_t ldb, T* x, int64_t ldx, int trans, int mode, T* w) {
+  cudaStream_t stream = ctx->stream;
+  int* flags = nullptr;
+  int* ticket = nullptr;
+  int rc = trsv_scratch(ctx, n, &flags, &ticket);
+  if (rc) return rc;
+  const int64_t ldw = nrhs;
+  const int64_t total = (int64_t)n * nrhs;
+  const int pblocks = (int)((total + 255) / 256);
+  const bool exact = (mode == LUHOT_MODE_EXACT);
+  // One triangular sweep of the LU factor over w (sync-free, one launch per
+  // 16 right-hand sides).
+  auto sweep = [&](bool lower, bool unit, bool tr, bool ex) -> int {
     prof_begin(ctx, kProfTrsv);
-    dk<<<1, 128, (size_t)bs * bs * sizeof(T), stream>>>(a, lda, x, ldx, j0, bs, nrhs);
-    prof_end(ctx, kProfTrsv, (double)bs * bs * nrhs, ((double)bs * bs / 2 + 2.0 * bs * nrhs) * sizeof(T));
-    const int i_begin = kLower ? j0 + bs : 0;
-    const int i_end = kLower ? n : j0;
-    if (i_end > i_begin) {
-      const size_t sm = ((size_t)64 * (bs + 1) + (size_t)bs * nrhs) * sizeof(T);
+    cudaError_t e = launch_trsv_syncfree<T>(stream, lu, lda, w, ldw, n, nrhs, lower, unit, tr, ex, flags, ticket,
+                                            ctx->d_status);
+    prof_end(ctx, kProfTrsv, (double)n * n * nrhs, ((double)n * n / 2 + 2.0 * total) * sizeof(T));
+    if (e != cudaSuccess) return set_error(ctx, LUHOT_ERR_CUDA, std::string("getrs sweep: ") + cudaGetErrorString(e));
+    return LUHOT_OK;
+  };
+  if (!trans) {
+    prof_begin(ctx, kProfPermute);
+    permute_rows_kernel<T, false><<<pblocks, 256, 0, stream>>>(b, ldb, w, ldw, perm, n, nrhs);
+    prof_end(ctx, kProfPermute, 0.0, 2.0 * total * sizeof(T));
+    rc = sweep(true, true, false, exact);
+    if (rc) return rc;
+    if (exact) {
+      const size_t xs = (size_t)n * sizeof(T);
+      const int use_smem = xs <= (size_t)ctx->max_smem_optin - 1024 ? 1 : 0;
+      LUHOT_CUDA_TRY(ctx, cudaFuncSetAttribute(back_exact_kernel<T>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               use_smem ? (int)xs : 0));
       prof_begin(ctx, kProfTrsv);
-      uk<<<(i_end - i_begin + 63) / 64, 256, sm, stream>>>(a, lda, x, ldx, j0, bs, i_begin, i_end, nrhs);
-      const double rows = (double)(i_end - i_begin);
-      prof_end(ctx, kProfTrsv, 2.0 * rows * bs * nrhs,
-               (rows * bs + 2.0 * rows * nrhs + (double)bs * nrhs) * sizeof(T));
+      back_exact_kernel<T><<<nrhs, 32, use_smem ? xs : 0, stream>>>(lu, lda, w, ldw, n, use_smem);
+      prof_end(ctx, kProfTrsv, (double)n * n * nrhs, ((double)n * n / 2 + 2.0 * total) * sizeof(T));
+    } else {
+      rc = sweep(false, false, false, false);
+      if (rc) return rc;
     }
+    {
+      int rc_ = copy_2d(ctx, x, ldx * sizeof(T), w, ldw * sizeof(T), nrhs * sizeof(T), n,
+                                          cudaMemcpyDeviceToDevice);
+      if (rc_) return rc_;
+    }
+  } else {
+    // A^T x = b:  U^T z = b (lower, non-unit), L^T y = z (upper, unit), x = P y.
+    {
+      int rc_ = copy_2d(ctx, w, ldw * sizeof(T), b, ldb * sizeof(T), nrhs * sizeof(T), n,
+                                          cudaMemcpyDeviceToDevice);
+      if (rc_) return rc_;
+    }
+    rc = sweep(true, false, true, false);
+    if (rc) return rc;
+    rc = sweep(false, true, true, false);
+    if (rc) return rc;
+    prof_begin(ctx, kProfPermute);
+    permute_rows_kernel<T, true><<<pblocks, 256, 0, stream>>>(w, ldw, x, ldx, perm, n, nrhs);
+    prof_end(ctx, kProfPermute, 0.0, 2.0 * total * sizeof(T));
   }
   LUHOT_CUDA_TRY(ctx, cudaGetLastError());
   return LUHOT_OK;
@@ -258,59 +299,25 @@ int getrs_device(luhot_ctx* ctx, int n, int nrhs, const T* lu, int64_t lda, cons
   if (n < 0 || nrhs < 0 || lda < std::max(1, n) || ldb < std::max(1, nrhs) || ldx < std::max(1, nrhs))
     return set_error(ctx, LUHOT_ERR_INVALID_ARG, "getrs: bad shape or leading dimension");
   if (n == 0 || nrhs == 0) return LUHOT_OK;
-  cudaStream_t stream = ctx->stream;
-  int rc = ensure_buf(ctx, ctx->perm_buf, (size_t)n * sizeof(int));
+  int rc = reset_status(ctx);
+  if (rc) return rc;
+  rc = ensure_buf(ctx, ctx->perm_buf, (size_t)n * sizeof(int));
   if (rc) return rc;
   int* perm = static_cast<int*>(ctx->perm_buf.ptr);
-  rc = launch_perm<T>(ctx, piv, n, perm, stream);
+  rc = getrs_perm(ctx, piv, n, perm);
   if (rc) return rc;
   // Work in a private buffer so that x may alias b.
   rc = ensure_buf(ctx, ctx->work[3], (size_t)n * nrhs * sizeof(T));
   if (rc) return rc;
-  T* w = static_cast<T*>(ctx->work[3].ptr);
-  const int64_t ldw = nrhs;
-  const int64_t total = (int64_t)n * nrhs;
-  const int pblocks = (int)((total + 255) / 256);
-  const bool exact = (mode == LUHOT_MODE_EXACT);
-  if (!trans) {
-    prof_begin(ctx, kProfPermute);
-    permute_rows_kernel<T, false><<<pblocks, 256, 0, stream>>>(b, ldb, w, ldw, perm, n, nrhs);
-    prof_end(ctx, kProfPermute, 0.0, 2.0 * total * sizeof(T));
-    if (exact) {
-      rc = blocked_trsv<T, true, true, true, false>(ctx, lu, lda, w, ldw, n, nrhs, stream);
-      if (rc) return rc;
-      const size_t xs = (size_t)n * sizeof(T);
-      const int use_smem = xs <= (size_t)ctx->max_smem_optin - 1024 ? 1 : 0;
-      LUHOT_CUDA_TRY(ctx, cudaFuncSetAttribute(back_exact_kernel<T>,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               use_smem ? (int)xs : 0));
-      prof_begin(ctx, kProfTrsv);
-      back_exact_kernel<T><<<nrhs, 32, use_smem ? xs : 0, stream>>>(lu, lda, w, ldw, n, use_smem);
-      prof_end(ctx, kProfTrsv, (double)n * n * nrhs, ((double)n * n / 2 + 2.0 * total) * sizeof(T));
-    } else {
-      rc = blocked_trsv<T, false, true, true, false>(ctx, lu, lda, w, ldw, n, nrhs, stream);
-      if (rc) return rc;
-      rc = blocked_trsv<T, false, false, false, false>(ctx, lu, lda, w, ldw, n, nrhs, stream);
-      if (rc) return rc;
-    }
-    LUHOT_CUDA_TRY(ctx, cudaMemcpy2DAsync(x, ldx * sizeof(T), w, ldw * sizeof(T), nrhs * sizeof(T), n,
-                                          cudaMemcpyDeviceToDevice, stream));
-  } else {
-    // A^T x = b:  U^T z = b (lower, non-unit), L^T y = z (upper, unit), x = P y.
-    LUHOT_CUDA_TRY(ctx, cudaMemcpy2DAsync(w, ldw * sizeof(T), b, ldb * sizeof(T), nrhs * sizeof(T), n,
-                                          cudaMemcpyDeviceToDevice, stream));
-    rc = blocked_trsv<T, false, true, false, true>(ctx, lu, lda, w, ldw, n, nrhs, stream);
-    if (rc) return rc;
-    rc = blocked_trsv<T, false, false, true, true>(ctx, lu, lda, w, ldw, n, nrhs, stream);
-    if (rc) return rc;
-    prof_begin(ctx, kProfPermute);
-    permute_rows_kernel<T, true><<<pblocks, 256, 0, stream>>>(w, ldw, x, ldx, perm, n, nrhs);
-    prof_end(ctx, kProfPermute, 0.0, 2.0 * total * sizeof(T));
-  }
-  LUHOT_CUDA_TRY(ctx, cudaGetLastError());
-  return LUHOT_OK;
+  rc = getrs_apply<T>(ctx, n, nrhs, lu, lda, perm, b, ldb, x, ldx, trans, mode, static_cast<T*>(ctx->work[3].ptr));
+  if (rc) return rc;
+  return finish_status(ctx, nullptr);
 }
 
+template int getrs_apply<double>(luhot_ctx*, int, int, const double*, int64_t, const int*, const double*, int64_t,
+                                 double*, int64_t, int, int, double*);
+template int getrs_apply<float>(luhot_ctx*, int, int, const float*, int64_t, const int*, const float*, int64_t,
+                                float*, int64_t, int, int, float*);
 template int getrs_device<double>(luhot_ctx*, int, int, const double*, int64_t, const int*,
                                   const double*, int64_t, double*, int64_t, int, int);
 template int getrs_device<float>(luhot_ctx*, int, int, const float*, int64_t, const int*,

@@ -1,0 +1,553 @@
+// Mixed-precision LU with iterative refinement (plain IR and GMRES-IR).
+//
+// The factorization runs in a low precision; FP64 is used only for the
+// residual r = b - A x, the update x += d and the backward-error test
+//   berr = ||r||_inf / (||A||_inf ||x||_inf + ||b||_inf)  <= tol (n * 2^-53 by default).
+//
+// Plain IR (Wilkinson / Moler): d = (LU)^-1 r in the low precision, x += d.
+// Converges when kappa(A) * u_low < 1 (FP32: kappa up to ~1e6).
+// GMRES-IR (Carson & Higham, SIAM J. Sci. Comput. 2017/2018): the correction
+// equation A d = r is solved by restarted GMRES in FP64 on the left-
+// preconditioned system (LU)^-1 A d = (LU)^-1 r, with the low-precision
+// factors applied in the low precision; classical Gram-Schmidt with one
+// reorthogonalisation pass; Givens rotations and the small least-squares
+// problem on the host.  It converges for much larger kappa * u_low.
+//
+// Every low-precision solve scales its right-hand side by its infinity norm
+// first (the scale stays on the device), so tiny residuals neither underflow
+// nor lose relative accuracy in the low precision.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+#include "luhot_internal.h"
+
+namespace luhot {
+
+__device__ __forceinline__ void atomic_max_nonneg(double* addr, double v) {
+  // Non-negative doubles order like their bit patterns; NaN sorts above inf.
+  atomicMax(reinterpret_cast<unsigned long long*>(addr), (unsigned long long)__double_as_longlong(v));
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, off));
+  return v;
+}
+
+template <typename Tlo>
+__device__ __forceinline__ Tlo to_low(double v) {
+  return static_cast<Tlo>(v);
+}
+
+// lo = A (rounded), anorm = max_i sum_j |a_ij|.  One warp per row.
+template <typename Tlo>
+__global__ void ir_convert_kernel(const double* __restrict__ a, int64_t lda, Tlo* lo, int64_t ldlo, int n,
+                                  double* anorm) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= n) return;
+  const double* row = a + (int64_t)warp * lda;
+  Tlo* out = lo + (int64_t)warp * ldlo;
+  double s = 0.0;
+  for (int c = lane; c < n; c += 32) {
+    const double v = row[c];
+    s += fabs(v);
+    out[c] = to_low<Tlo>(v);
+  }
+  s = warp_sum(s);
+  if (lane == 0) atomic_max_nonneg(anorm, s);
+}
+
+// kResidual: r = b - A x and rnorm = max |r_i|;  otherwise r = A x.
+// One warp per row, FP64 FMA, x read through L1/L2 (n doubles).
+template <bool kResidual>
+__global__ void ir_matvec_kernel(const double* __restrict__ a, int64_t lda, const double* __restrict__ x,
+                                 const double* __restrict__ b, double* r, int n, double* rnorm) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= n) return;
+  const double* row = a + (int64_t)warp * lda;
+  double s0 = 0.0, s1 = 0.0;
+  int c = lane * 2;
+  if ((reinterpret_cast<uintptr_t>(row) & 15) == 0) {
+    for (; c + 1 < n; c += 64) {
+      const double2 v = *reinterpret_cast<const double2*>(row + c);
+      s0 = fma(v.x, x[c], s0);
+      s1 = fma(v.y, x[c + 1], s1);
+    }
+    if (c < n) s0 = fma(row[c], x[c], s0);
+  } else {
+    for (int cc = lane; cc < n; cc += 32) s0 = fma(row[cc], x[cc], s0);
+  }
+  const double s = warp_sum(s0 + s1);
+  if (lane == 0) {
+    if (kResidual) {
+      const double ri = b[warp] - s;
+      r[warp] = ri;
+      atomic_max_nonneg(rnorm, fabs(ri));
+    } else {
+      r[warp] = s;
+    }
+  }
+}
+
+__global__ void ir_infnorm_kernel(const double* __restrict__ v, int n, double* out) {
+  double m = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) m = fmax(m, fabs(v[i]));
+  m = warp_max(m);
+  if ((threadIdx.x & 31) == 0) atomic_max_nonneg(out, m);
+}
+
+// lo = v / scale (scale = *sc, or 1 when it is 0).
+template <typename Tlo>
+__global__ void ir_to_low_kernel(const double* __restrict__ v, Tlo* lo, int n, const double* sc) {
+  const double s = *sc;
+  const double inv = (s > 0.0 && isfinite(s)) ? 1.0 / s : 1.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    lo[i] = to_low<Tlo>(v[i] * inv);
+}
+
+// out = lo * scale   or (kAdd) x += lo * scale with xnorm = max |x|.
+template <typename Tlo, bool kAdd>
+__global__ void ir_from_low_kernel(const Tlo* __restrict__ lo, double* out, int n, const double* sc, double* xnorm) {
+  const double s = *sc;
+  const double mul = (s > 0.0 && isfinite(s)) ? s : 1.0;
+  double m = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double d = static_cast<double>(lo[i]) * mul;
+    if (kAdd) {
+      const double xi = out[i] + d;
+      out[i] = xi;
+      m = fmax(m, fabs(xi));
+    } else {
+      out[i] = d;
+    }
+  }
+  if (kAdd) {
+    m = warp_max(m);
+    if ((threadIdx.x & 31) == 0) atomic_max_nonneg(xnorm, m);
+  }
+}
+
+// h[j] += sum_i V_j[i] w[i] for j < k  (V_j contiguous, n each).
+__global__ void ir_dots_kernel(const double* __restrict__ V, int k, const double* __restrict__ w, double* h, int n) {
+  __shared__ double part[32][8];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int j0 = 0; j0 < k; j0 += 8) {
+    double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+      const double wi = w[i];
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (j0 + q < k) acc[q] = fma(V[(int64_t)(j0 + q) * n + i], wi, acc[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const double s = warp_sum(acc[q]);
+      if (lane == 0) part[wid][q] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x < 8 && j0 + threadIdx.x < k) {
+      double s = 0.0;
+      for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += part[q][threadIdx.x];
+      atomicAdd(&h[j0 + threadIdx.x], s);
+    }
+    __syncthreads();
+  }
+}
+
+// w -= sum_j V_j h_j (j < k);  if nrm2 != nullptr, also nrm2 += sum w_i^2.
+__global__ void ir_orth_kernel(const double* __restrict__ V, int k, const double* __restrict__ h, double* w, int n,
+                               double* nrm2) {
+  double sq = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double wi = w[i];
+    for (int j = 0; j < k; ++j) wi = fma(-V[(int64_t)j * n + i], h[j], wi);
+    w[i] = wi;
+    sq = fma(wi, wi, sq);
+  }
+  if (nrm2) {
+    sq = warp_sum(sq);
+    if ((threadIdx.x & 31) == 0) atomicAdd(nrm2, sq);
+  }
+}
+
+// dst = src * (1 / *den)   (den = a 2-norm, taken as sqrt here when kSqrt).
+template <bool kSqrt>
+__global__ void ir_scale_kernel(const double* src, double* dst, int n, const double* den) {
+  const double d = kSqrt ? sqrt(*den) : *den;
+  const double inv = d > 0.0 ? 1.0 / d : 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[i] = src[i] * inv;
+}
+
+// x += sum_j V_j y_j, xnorm = max |x|.
+__global__ void ir_combine_kernel(const double* __restrict__ V, int k, const double* __restrict__ y, double* x, int n,
+                                  double* xnorm) {
+  double m = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double xi = x[i];
+    for (int j = 0; j < k; ++j) xi = fma(V[(int64_t)j * n + i], y[j], xi);
+    x[i] = xi;
+    m = fmax(m, fabs(xi));
+  }
+  m = warp_max(m);
+  if ((threadIdx.x & 31) == 0) atomic_max_nonneg(xnorm, m);
+}
+
+// ---------------------------------------------------------------------------
+// Driver.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int kGmresRestart = 40;
+constexpr double kGmresTol = 1e-6;  // relative reduction of the preconditioned residual per solve
+
+// Device scalars.
+enum Sc : int { kAnorm = 0, kBnorm, kRnorm, kXnorm, kVscale, kNrm2, kH = 8 };
+
+template <typename Tlo>
+struct IrRun {
+  luhot_ctx* ctx;
+  int n;
+  const double* a;
+  int64_t lda;
+  Tlo* lu;
+  int64_t ldlo;
+  int* piv;
+  int* perm;
+  Tlo* lo1;
+  Tlo* lo2;
+  Tlo* low;    // getrs scratch
+  double* r;   // residual / Arnoldi work
+  double* t;   // second FP64 work vector
+  double* V;   // (restart + 1) x n
+  double* sc;  // device scalars
+  double* hsc; // pinned host mirror of sc
+  int grid_vec;
+
+  int launch_check(const char* what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return set_error(ctx, LUHOT_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    return LUHOT_OK;
+  }
+
+  int zero_scalar(int idx, int count = 1) {
+    LUHOT_CUDA_TRY(ctx, cudaMemsetAsync(sc + idx, 0, sizeof(double) * count, ctx->stream));
+    return LUHOT_OK;
+  }
+
+  int read_scalars(int count) {
+    LUHOT_CUDA_TRY(ctx, cudaMemcpyAsync(hsc, sc, sizeof(double) * count, cudaMemcpyDeviceToHost, ctx->stream));
+    LUHOT_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    return LUHOT_OK;
+  }
+
+  // out (FP64) = (LU)^-1 v, through the low precision with infinity-norm scaling.
+  int lo_solve(const double* v, double* out, bool add_into_out) {
+    int rc = zero_scalar(kVscale);
+    if (rc) return rc;
+    prof_begin(ctx, kProfRefine);
+    ir_infnorm_kernel<<<grid_vec, 256, 0, ctx->stream>>>(v, n, sc + kVscale);
+    prof_end(ctx, kProfRefine, 0.0, 8.0 * n);
+    prof_begin(ctx, kProfRefine);
+    ir_to_low_kernel<Tlo><<<grid_vec, 256, 0, ctx->stream>>>(v, lo1, n, sc + kVscale);
+    prof_end(ctx, kProfRefine, 0.0, (8.0 + sizeof(Tlo)) * n);
+    rc = launch_check("ir to-low");
+    if (rc) return rc;
+    rc = getrs_apply<Tlo>(ctx, n, 1, lu, ldlo, perm, lo1, 1, lo2, 1, 0, LUHOT_MODE_FAST, low);
+    if (rc) return rc;
+    prof_begin(ctx, kProfRefine);
+    if (add_into_out) {
+      ir_from_low_kernel<Tlo, true><<<grid_vec, 256, 0, ctx->stream>>>(lo2, out, n, sc + kVscale, sc + kXnorm);
+    } else {
+      ir_from_low_kernel<Tlo, false><<<grid_vec, 256, 0, ctx->stream>>>(lo2, out, n, sc + kVscale, nullptr);
+    }
+    prof_end(ctx, kProfRefine, (double)n, (sizeof(Tlo) + 16.0) * n);
+    return launch_check("ir from-low");
+  }
+
+  int residual(const double* b, const double* x) {
+    int rc = zero_scalar(kRnorm);
+    if (rc) return rc;
+    const int blocks = (n + 7) / 8;
+    prof_begin(ctx, kProfRefine);
+    ir_matvec_kernel<true><<<blocks, 256, 0, ctx->stream>>>(a, lda, x, b, r, n, sc + kRnorm);
+    prof_end(ctx, kProfRefine, 2.0 * n * n, 8.0 * n * (double)n + 24.0 * n);
+    return launch_check("ir residual");
+  }
+
+  int matvec(const double* x, double* y) {
+    const int blocks = (n + 7) / 8;
+    prof_begin(ctx, kProfRefine);
+    ir_matvec_kernel<false><<<blocks, 256, 0, ctx->stream>>>(a, lda, x, nullptr, y, n, nullptr);
+    prof_end(ctx, kProfRefine, 2.0 * n * n, 8.0 * n * (double)n + 16.0 * n);
+    return launch_check("ir matvec");
+  }
+
+  // One GMRES cycle for A d = r (left-preconditioned), x += d.  Returns the
+  // number of inner iterations through *inner.
+  int gmres_cycle(double* x, int* inner) {
+    const int m = kGmresRestart;
+    // v0 = M^-1 r / ||M^-1 r||_2
+    int rc = lo_solve(r, t, false);
+    if (rc) return rc;
+    rc = zero_scalar(kNrm2);
+    if (rc) return rc;
+    ir_orth_kernel<<<grid_vec, 256, 0, ctx->stream>>>(V, 0, sc + kH, t, n, sc + kNrm2);
+    ir_scale_kernel<true><<<grid_vec, 256, 0, ctx->stream>>>(t, V, n, sc + kNrm2);
+    count_launch(ctx, 2);
+    rc = read_scalars(kH);
+    if (rc) return rc;
+    const double beta = std::sqrt(hsc[kNrm2]);
+    if (!(beta > 0.0) || !std::isfinite(beta)) {
+      *inner = 0;
+      return LUHOT_OK;
+    }
+    std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m), sn(m), g(m + 1, 0.0);
+    g[0] = beta;
+    int k = 0;
+    for (; k < m; ++k) {
+      double* vk = V + (int64_t)k * n;
+      double* vk1 = V + (int64_t)(k + 1) * n;
+      rc = matvec(vk, r);  // r is free as scratch inside the cycle
+      if (rc) return rc;
+      rc = lo_solve(r, vk1, false);
+      if (rc) return rc;
+      // Two passes of classical Gram-Schmidt against v_0..v_k.
+      std::vector<double> hcol(k + 2, 0.0);
+      for (int pass = 0; pass < 2; ++pass) {
+        rc = zero_scalar(kH, k + 1);
+        if (rc) return rc;
+        if (pass == 1) {
+          rc = zero_scalar(kNrm2);
+          if (rc) return rc;
+        }
+        ir_dots_kernel<<<std::min(grid_vec, 256), 256, 0, ctx->stream>>>(V, k + 1, vk1, sc + kH, n);
+        ir_orth_kernel<<<grid_vec, 256, 0, ctx->stream>>>(V, k + 1, sc + kH, vk1, n, pass == 1 ? sc + kNrm2 : nullptr);
+        count_launch(ctx, 2);
+        rc = read_scalars(kH + k + 1);
+        if (rc) return rc;
+        for (int j = 0; j <= k; ++j) hcol[j] += hsc[kH + j];
+      }
+      const double hnext = std::sqrt(hsc[kNrm2]);
+      hcol[k + 1] = hnext;
+      // v_{k+1} = w / ||w||_2 (sc[kNrm2] holds sum w_i^2 of the second pass)
+      ir_scale_kernel<true><<<grid_vec, 256, 0, ctx->stream>>>(vk1, vk1, n, sc + kNrm2);
+      count_launch(ctx);
+      // Givens rotations on column k.
+      for (int j = 0; j < k; ++j) {
+        const double t0 = cs[j] * hcol[j] + sn[j] * hcol[j + 1];
+        hcol[j + 1] = -sn[j] * hcol[j] + cs[j] * hcol[j + 1];
+        hcol[j] = t0;
+      }
+      const double den = std::hypot(hcol[k], hcol[k + 1]);
+      cs[k] = den > 0.0 ? hcol[k] / den : 1.0;
+      sn[k] = den > 0.0 ? hcol[k + 1] / den : 0.0;
+      hcol[k] = den;
+      hcol[k + 1] = 0.0;
+      g[k + 1] = -sn[k] * g[k];
+      g[k] = cs[k] * g[k];
+      for (int j = 0; j <= k; ++j) H[(size_t)j * m + k] = hcol[j];
+      if (std::fabs(g[k + 1]) <= kGmresTol * beta || !(hnext > 0.0)) {
+        ++k;
+        break;
+      }
+    }
+    // Solve the k x k upper-triangular system H y = g.
+    std::vector<double> y(k, 0.0);
+    for (int i = k - 1; i >= 0; --i) {
+      double s = g[i];
+      for (int j = i + 1; j < k; ++j) s -= H[(size_t)i * m + j] * y[j];
+      y[i] = H[(size_t)i * m + i] != 0.0 ? s / H[(size_t)i * m + i] : 0.0;
+    }
+    for (int i = 0; i < k; ++i) hsc[kH + i] = y[i];
+    LUHOT_CUDA_TRY(ctx, cudaMemcpyAsync(sc + kH, hsc + kH, sizeof(double) * k, cudaMemcpyHostToDevice, ctx->stream));
+    rc = zero_scalar(kXnorm);
+    if (rc) return rc;
+    ir_combine_kernel<<<grid_vec, 256, 0, ctx->stream>>>(V, k, sc + kH, x, n, sc + kXnorm);
+    count_launch(ctx);
+    *inner = k;
+    return launch_check("gmres combine");
+  }
+};
+
+}  // namespace
+
+template <typename Tlo>
+static int gesv_ir_impl(luhot_ctx* ctx, int n, const double* a, int64_t lda, const double* b, double* x,
+                        int solver, double tol, int max_iter, luhot_ir_info* info) {
+  cudaStream_t stream = ctx->stream;
+  const int64_t ldlo = ((int64_t)n + 63) / 64 * 64;
+  int rc = ensure_buf(ctx, ctx->ir_buf[0], (size_t)n * ldlo * sizeof(Tlo));
+  if (rc) return rc;
+  const size_t vecs = (size_t)n * sizeof(double);
+  rc = ensure_buf(ctx, ctx->ir_buf[1], vecs * (2 + kGmresRestart + 1) + 3 * (size_t)n * sizeof(Tlo) + 4096);
+  if (rc) return rc;
+  const size_t idx_ints = (2 * (size_t)n + 63) / 64 * 64;  // pivots + permutation, 256-byte aligned end
+  rc = ensure_buf(ctx, ctx->ir_buf[2], idx_ints * sizeof(int) + 256 * sizeof(double));
+  if (rc) return rc;
+  IrRun<Tlo> s;
+  s.ctx = ctx;
+  s.n = n;
+  s.a = a;
+  s.lda = lda;
+  s.lu = static_cast<Tlo*>(ctx->ir_buf[0].ptr);
+  s.ldlo = ldlo;
+  char* base = static_cast<char*>(ctx->ir_buf[1].ptr);
+  s.r = reinterpret_cast<double*>(base);
+  s.t = s.r + n;
+  s.V = s.t + n;
+  s.lo1 = reinterpret_cast<Tlo*>(s.V + (size_t)(kGmresRestart + 1) * n);
+  s.lo2 = s.lo1 + n;
+  s.low = s.lo2 + n;
+  s.piv = static_cast<int*>(ctx->ir_buf[2].ptr);
+  s.perm = s.piv + n;
+  s.sc = reinterpret_cast<double*>(s.piv + idx_ints);
+  s.hsc = ctx->h_scalars;
+  s.grid_vec = std::min(ctx->num_sms * 4, (n + 255) / 256);
+
+  cudaEvent_t e0, e1, e2;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventCreate(&e2);
+  struct EvGuard {
+    cudaEvent_t a, b, c;
+    ~EvGuard() {
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+      cudaEventDestroy(c);
+    }
+  } guard{e0, e1, e2};
+  cudaEventRecord(e0, stream);
+
+  // 1. FP64 -> low precision, ||A||_inf.
+  LUHOT_CUDA_TRY(ctx, cudaMemsetAsync(s.sc, 0, 64 * sizeof(double), stream));
+  prof_begin(ctx, kProfRefine);
+  ir_convert_kernel<Tlo><<<(n + 7) / 8, 256, 0, stream>>>(a, lda, s.lu, ldlo, n, s.sc + kAnorm);
+  prof_end(ctx, kProfRefine, (double)n * n, (8.0 + sizeof(Tlo)) * n * (double)n);
+  rc = s.launch_check("ir convert");
+  if (rc) return rc;
+  // 2. Low-precision LU.
+  int64_t sing = -1;
+  rc = getrf_device<Tlo>(ctx, n, n, s.lu, ldlo, s.piv, LUHOT_MODE_FAST, &sing);
+  if (rc) return rc;
+  info->singular = sing;
+  if (sing >= 0) return set_error(ctx, LUHOT_ERR_SINGULAR, "the low-precision factor is singular");
+  rc = getrs_perm(ctx, s.piv, n, s.perm);
+  if (rc) return rc;
+  cudaEventRecord(e1, stream);
+
+  // 3. ||b||_inf and the first solve x0 = (LU)^-1 b.
+  prof_begin(ctx, kProfRefine);
+  ir_infnorm_kernel<<<s.grid_vec, 256, 0, stream>>>(b, n, s.sc + kBnorm);
+  prof_end(ctx, kProfRefine, 0.0, 8.0 * n);
+  rc = s.lo_solve(b, x, false);
+  if (rc) return rc;
+
+  const double tol_eff = tol > 0.0 ? tol : n * std::ldexp(1.0, -53);
+  int it = 0, inner_total = 0;
+  double berr = INFINITY, prev = INFINITY;
+  bool converged = false;
+  int stall = 0;
+  for (;;) {
+    rc = s.zero_scalar(kXnorm);
+    if (rc) return rc;
+    prof_begin(ctx, kProfRefine);
+    ir_infnorm_kernel<<<s.grid_vec, 256, 0, stream>>>(x, n, s.sc + kXnorm);
+    prof_end(ctx, kProfRefine, 0.0, 8.0 * n);
+    rc = s.residual(b, x);
+    if (rc) return rc;
+    rc = s.read_scalars(kVscale);
+    if (rc) return rc;
+    const double anorm = s.hsc[kAnorm], bnorm = s.hsc[kBnorm], rnorm = s.hsc[kRnorm], xnorm = s.hsc[kXnorm];
+    berr = rnorm / (anorm * xnorm + bnorm);
+    if (!std::isfinite(berr)) berr = INFINITY;
+    if (berr <= tol_eff) {
+      converged = true;
+      break;
+    }
+    if (it >= max_iter) break;
+    // Stop when the iteration no longer contracts (plain IR diverging, or
+    // stagnation at the attainable accuracy).
+    if (berr > 0.9 * prev) {
+      if (++stall >= 2) break;
+    } else {
+      stall = 0;
+    }
+    prev = std::min(prev, berr);
+    if (solver == LUHOT_REFINE_GMRES) {
+      int inner = 0;
+      rc = s.gmres_cycle(x, &inner);
+      if (rc) return rc;
+      inner_total += inner;
+    } else {
+      rc = s.lo_solve(s.r, x, true);
+      if (rc) return rc;
+    }
+    ++it;
+  }
+  cudaEventRecord(e2, stream);
+  LUHOT_CUDA_TRY(ctx, cudaEventSynchronize(e2));
+  float f_ms = 0.f, r_ms = 0.f;
+  cudaEventElapsedTime(&f_ms, e0, e1);
+  cudaEventElapsedTime(&r_ms, e1, e2);
+  info->iterations = std::max(info->iterations, it);
+  info->inner_iterations += inner_total;
+  info->backward_error = std::max(info->backward_error, berr);
+  info->factor_ms += f_ms;
+  info->refine_ms += r_ms;
+  info->converged = info->converged && converged;
+  return LUHOT_OK;
+}
+
+int gesv_ir_device(luhot_ctx* ctx, int n, int nrhs, const double* a, int64_t lda, const double* b, int64_t ldb,
+                   double* x, int64_t ldx, int precision, int solver, double tol, int max_iter,
+                   luhot_ir_info* info) {
+  if (n < 0 || nrhs < 0 || lda < std::max(1, n) || ldb < std::max(1, nrhs) || ldx < std::max(1, nrhs))
+    return set_error(ctx, LUHOT_ERR_INVALID_ARG, "gesv_ir: bad shape or leading dimension");
+  if (solver != LUHOT_REFINE_IR && solver != LUHOT_REFINE_GMRES)
+    return set_error(ctx, LUHOT_ERR_INVALID_ARG, "gesv_ir: unknown solver");
+  if (max_iter < 0) return set_error(ctx, LUHOT_ERR_INVALID_ARG, "gesv_ir: negative max_iter");
+  *info = luhot_ir_info{};
+  info->converged = 1;
+  info->precision = precision;
+  info->solver = solver;
+  info->singular = -1;
+  if (n == 0 || nrhs == 0) return LUHOT_OK;
+  if (precision != LUHOT_PREC_FP32)
+    return set_error(ctx, LUHOT_ERR_UNSUPPORTED, "gesv_ir: only the FP32 factorization is built");
+  int rc = reset_status(ctx);
+  if (rc) return rc;
+  // Columns of b and x are strided (ld); the driver works on contiguous vectors.
+  rc = ensure_buf(ctx, ctx->ir_buf[3], (size_t)n * 2 * sizeof(double));
+  if (rc) return rc;
+  double* bc = static_cast<double*>(ctx->ir_buf[3].ptr);
+  double* xc = bc + n;
+  for (int c = 0; c < nrhs; ++c) {
+    {
+      int rc_ = copy_2d(ctx, bc, sizeof(double), b + c, ldb * sizeof(double), sizeof(double), n,
+                                          cudaMemcpyDeviceToDevice);
+      if (rc_) return rc_;
+    }
+    rc = gesv_ir_impl<float>(ctx, n, a, lda, bc, xc, solver, tol, max_iter, info);
+    if (rc) return rc;
+    {
+      int rc_ = copy_2d(ctx, x + c, ldx * sizeof(double), xc, sizeof(double), sizeof(double), n,
+                                          cudaMemcpyDeviceToDevice);
+      if (rc_) return rc_;
+    }
+  }
+  rc = finish_status(ctx, nullptr);
+  if (rc) return rc;
+  if (!info->converged)
+    return set_error(ctx, LUHOT_ERR_NOT_CONVERGED,
+                     "refinement stopped at backward error " + std::to_string(info->backward_error));
+  return LUHOT_OK;
+}
+
+}  // namespace luhot

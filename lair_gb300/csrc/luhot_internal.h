@@ -59,6 +59,9 @@ struct luhot_ctx {
   luhot::DevBuf work[4];                    // matrix / rhs / solution / misc
   luhot::DevBuf piv_buf;                    // int32 pivots
   luhot::DevBuf perm_buf;                   // int32 permutation
+  luhot::DevBuf trsv_buf;                   // ready flags + ticket of the triangular sweeps
+  luhot::DevBuf ir_buf[4];                  // refinement: low-precision LU, vectors, indices, rhs
+  double* h_scalars = nullptr;              // pinned: scalars read back by the refinement loop
   void* h_piv = nullptr;                    // pinned pivots staging
   size_t h_piv_bytes = 0;
   int nb_override = 0;
@@ -78,6 +81,10 @@ int reset_status(luhot_ctx* ctx);
 // Synchronises the stream, reads the device status; fills *singular.
 int finish_status(luhot_ctx* ctx, int64_t* singular);
 int ensure_buf(luhot_ctx* ctx, DevBuf& b, size_t bytes);
+// Row-pitched copy on the context's stream: one linear copy when both sides
+// are contiguous, a kernel for strided device-to-device, else cudaMemcpy2DAsync.
+int copy_2d(luhot_ctx* ctx, void* dst, size_t dpitch, const void* src, size_t spitch, size_t wbytes, size_t rows,
+            cudaMemcpyKind kind);
 
 template <typename T>
 int getrf_device(luhot_ctx* ctx, int m, int n, T* a, int64_t lda, int* piv, int mode,
@@ -85,9 +92,21 @@ int getrf_device(luhot_ctx* ctx, int m, int n, T* a, int64_t lda, int* piv, int 
 
 // Solve with device factors: X (n x nrhs, ldx) <- op(A)^-1 B.  b and x may be
 // the same buffer.
+int gesv_ir_device(luhot_ctx* ctx, int n, int nrhs, const double* a, int64_t lda, const double* b, int64_t ldb,
+                   double* x, int64_t ldx, int precision, int solver, double tol, int max_iter,
+                   luhot_ir_info* info);
+
 template <typename T>
 int getrs_device(luhot_ctx* ctx, int n, int nrhs, const T* lu, int64_t lda, const int* piv,
                  const T* b, int64_t ldb, T* x, int64_t ldx, int trans, int mode);
+
+// getrs in two parts: compose the interchanges into a permutation once
+// (getrs_perm), then apply any number of solves with it (getrs_apply, async;
+// w is n x nrhs scratch that must not alias b or x).
+int getrs_perm(luhot_ctx* ctx, const int* piv, int n, int* perm);
+template <typename T>
+int getrs_apply(luhot_ctx* ctx, int n, int nrhs, const T* lu, int64_t lda, const int* perm, const T* b,
+                int64_t ldb, T* x, int64_t ldx, int trans, int mode, T* w);
 
 inline void count_launch(luhot_ctx* ctx, int64_t k = 1) { ctx->launches.fetch_add(k); }
 

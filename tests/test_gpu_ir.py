@@ -1,0 +1,76 @@
+"""Mixed-precision LU + iterative refinement against the FP64 oracle.
+
+Matrices follow the benchmark's construction at test sizes:
+A = Q1 diag(sigma) Q2^T with Q1, Q2 from Householder QR of seeded N(0,1)
+matrices and sigma geometric from 1 to 1/kappa.  Every result must reach the
+normwise backward error n * 2^-53; the forward error against lair's FP64
+solution (the oracle) is bounded by kappa * n * 2^-53 up to a small factor.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from lair_gb300 import _lib, refine
+from lair_gb300.errors import InvalidInput
+
+pytestmark = pytest.mark.gpu
+EPS64 = 2.0 ** -53
+
+
+def conditioned(n, kappa, seed):
+    rng = np.random.default_rng(seed)
+    q1, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    q2, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    sigma = np.geomspace(1.0, 1.0 / kappa, n)
+    return (q1 * sigma) @ q2.T
+
+
+def berr(a, x, b):
+    r = b - a @ x
+    return np.abs(r).max() / (np.abs(a).sum(1).max() * np.abs(x).max() + np.abs(b).max())
+
+
+@pytest.mark.parametrize("kappa", [1e2, 1e4, 1e6])
+@pytest.mark.parametrize("solver", ["ir", "gmres"])
+def test_fp32_refinement_reaches_fp64_backward_error(kappa, solver):
+    n = 1024
+    a = conditioned(n, kappa, 1)
+    b = np.random.default_rng(2).standard_normal(n)
+    x, info = refine.gesv_ir(a, b, precision="fp32", solver=solver)
+    assert info["converged"] == 1
+    assert berr(a, x, b) <= n * EPS64
+    assert info["backward_error"] <= n * EPS64
+    ref = a.copy()
+    piv, _ = oracle.getrf(ref)
+    x_ref = oracle.getrs(ref, piv, b)
+    rel = np.abs(x - x_ref).max() / np.abs(x_ref).max()
+    assert rel <= 50 * kappa * n * EPS64
+    if solver == "gmres":
+        assert info["inner_iterations"] >= info["iterations"]
+
+
+def test_refinement_multiple_rhs_and_strides():
+    n = 600
+    a = conditioned(n, 1e3, 3)
+    b = np.random.default_rng(4).standard_normal((n, 3))
+    x, info = refine.gesv_ir(np.asfortranarray(a), b)
+    for c in range(3):
+        assert berr(a, x[:, c], b[:, c]) <= n * EPS64
+    assert info["converged"] == 1
+
+
+def test_refinement_reports_non_convergence_for_hopeless_kappa():
+    n = 512
+    a = conditioned(n, 1e14, 5)
+    b = np.random.default_rng(6).standard_normal(n)
+    x, info = refine.gesv_ir(a, b, solver="ir", max_iter=5, raise_on_failure=False)
+    assert info["converged"] == 0
+    with pytest.raises(_lib.LuhotError):
+        refine.gesv_ir(a, b, solver="ir", max_iter=5)
+
+
+def test_refinement_errors():
+    with pytest.raises(InvalidInput.Shape):
+        refine.gesv_ir(np.zeros((3, 4)), np.zeros(3))
+    with pytest.raises(InvalidInput.Value):
+        refine.gesv_ir(np.zeros((4, 4)), np.ones(4))
