@@ -329,6 +329,11 @@ def run_ours(args):
         torch.cuda.empty_cache()
         ir = run_ir(args, lib, ctx, torch, rank)
 
+    batched_res = None
+    if not args.no_batched:
+        torch.cuda.empty_cache()
+        batched_res = run_batched(args, lib, ctx, torch)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_baseline(n, args.cpu_seconds)
@@ -340,7 +345,8 @@ def run_ours(args):
                 "config": workload_config(args), "backward_error": berr, "berr_bound": n * EPS64,
                 "berr_ok": berr <= n * EPS64, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                 "clocks": clocks.summary(), "gpu_launches": int(launches),
-                "kernel_profile_ms": {k: round(v["ms"], 3) for k, v in prof.items()}, "ir": ir}
+                "kernel_profile_ms": {k: round(v["ms"], 3) for k, v in prof.items()}, "ir": ir,
+                "batched": batched_res}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -425,6 +431,86 @@ def run_ir(args, lib, ctx, torch, rank):
             "speedup_vs_fp64": fp64_ms / results[best]["ms"], "berr_bound": n * EPS64}
 
 
+def run_batched(args, lib, ctx, torch):
+    """10,000 uneven systems (n ~ U{8..256}, A iid U[-1,1] + n*I with prob. 1/2,
+    one rhs iid U[-1,1]) in one graph-replayed persistent launch, FP64 and
+    FP32, against looping the plain single-system kernels over a sample."""
+    import ctypes
+
+    from lair_gb300 import _lib, batched
+
+    out = {}
+    for name, dt, tdt in (("f64", np.float64, torch.float64), ("f32", np.float32, torch.float32)):
+        sizes, a0, b0 = batched.synthetic_batch(args.batch_count, seed=11, dtype=dt)
+        solver = batched.BatchSolver(sizes, dtype=dt, mode="fast")
+        A0 = torch.from_numpy(a0).cuda()
+        B0 = torch.from_numpy(b0).cuda()
+        A, B = A0.clone(), B0.clone()
+        piv = torch.zeros(int(sizes.sum()), dtype=torch.int32, device="cuda")
+        info = torch.zeros(len(sizes), dtype=torch.int32, device="cuda")
+        t0 = time.perf_counter()
+        solver.autotune(A0.data_ptr(), B0.data_ptr())
+        tune_s = time.perf_counter() - t0
+
+        def step():
+            A.copy_(A0)
+            B.copy_(B0)
+            solver.solve_device(A.data_ptr(), B.data_ptr(), piv.data_ptr(), info.data_ptr())
+
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        stream = torch.cuda.current_stream()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        # worst backward error over the batch (FP64 check on the host)
+        x = B.cpu().numpy()
+        worst, ao, bo = 0.0, 0, 0
+        for n in sizes:
+            M = a0[ao:ao + n * n].reshape(n, n).astype(np.float64)
+            xx, bb = x[bo:bo + n].astype(np.float64), b0[bo:bo + n].astype(np.float64)
+            worst = max(worst, np.abs(bb - M @ xx).max() / (np.abs(M).sum(1).max() * np.abs(xx).max() + np.abs(bb).max()))
+            ao += int(n) * int(n)
+            bo += int(n)
+        # baseline: plain single-system getrf + getrs per system, on a sample
+        rng = np.random.default_rng(5)
+        sample = rng.choice(len(sizes), size=min(args.batch_loop_sample, len(sizes)), replace=False)
+        aoff = np.concatenate([[0], np.cumsum(sizes.astype(np.int64) ** 2)])
+        boff = np.concatenate([[0], np.cumsum(sizes.astype(np.int64))])
+        pre = "d" if dt == np.float64 else "s"
+        getrf, getrs = getattr(lib, f"luhot_{pre}getrf_dev"), getattr(lib, f"luhot_{pre}getrs_dev")
+        A.copy_(A0)
+        B.copy_(B0)
+        torch.cuda.synchronize()
+        sing = ctypes.c_int64(0)
+        es = A.element_size()
+        t0 = time.perf_counter()
+        for i in sample:
+            n = int(sizes[i])
+            pa = A.data_ptr() + int(aoff[i]) * es
+            pb = B.data_ptr() + int(boff[i]) * es
+            pp = piv.data_ptr() + int(boff[i]) * 4
+            _lib.check(getrf(ctx, n, n, pa, n, pp, ctypes.byref(sing), 0), ctx)
+            _lib.check(getrs(ctx, n, 1, pa, n, pp, pb, 1, 0, 0), ctx)
+        torch.cuda.synchronize()
+        loop_s = time.perf_counter() - t0
+        loop_rate = len(sample) / loop_s
+        fl = float(np.sum(2.0 / 3.0 * sizes.astype(np.float64) ** 3 + 2.0 * sizes.astype(np.float64) ** 2))
+        out[name] = {"systems": len(sizes), "ms_per_batch": ms, "systems_per_s": len(sizes) / (ms * 1e-3),
+                     "gflops": fl / (ms * 1e-3) / 1e9, "worst_backward_error": worst,
+                     "loop_single_system_systems_per_s": loop_rate,
+                     "loop_sample": f"{len(sample)} systems drawn from the batch, getrf_dev + getrs_dev each",
+                     "speedup_vs_loop": (len(sizes) / (ms * 1e-3)) / loop_rate, "autotune_s": tune_s,
+                     "tuning": solver.tuning()}
+        del A0, B0, A, B
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -440,6 +526,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-elim-steps", type=int, default=4)
     ap.add_argument("--no-ir", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batch-count", type=int, default=10000)
+    ap.add_argument("--batch-loop-sample", type=int, default=300)
     ap.add_argument("--ir-n", type=int, default=16384)
     ap.add_argument("--ir-kappa", type=float, default=1e6)
     args = ap.parse_args()

@@ -164,6 +164,51 @@ int luhot_dgesv_ir(luhot_ctx* ctx, int64_t n, int64_t nrhs, const double* a, int
                    const double* b, int64_t b_rs, int64_t b_cs, double* x, int64_t x_rs, int64_t x_cs,
                    int precision, int solver, double tol, int max_iter, luhot_ir_info* info);
 
+/* ---- Adjoint of the solve ----------------------------------------------
+ * No lair counterpart (lair has no differentiation).  For X = A^-1 B and a
+ * scalar loss with upstream gradient W = dL/dX (n x nrhs):
+ *   lambda = A^-T W  (transposed getrs on the stored factors and pivots),
+ *   dB = lambda,  dA = -lambda X^T  (skipped when dA is NULL). */
+int luhot_dgesv_backward(luhot_ctx* ctx, int64_t n, int64_t nrhs, const double* lu, int64_t lu_rs,
+                         int64_t lu_cs, const uint64_t* piv, const double* x, int64_t x_rs, int64_t x_cs,
+                         const double* w, int64_t w_rs, int64_t w_cs, double* db, int64_t db_rs,
+                         int64_t db_cs, double* da, int64_t da_rs, int64_t da_cs, int mode);
+/* Device-resident form: factors (lda) and int32 pivots from luhot_dgetrf_dev. */
+int luhot_dgesv_backward_dev(luhot_ctx* ctx, int64_t n, int64_t nrhs, const double* d_lu, int64_t lda,
+                             const int32_t* d_piv, const double* d_x, int64_t ldx, const double* d_w,
+                             int64_t ldw, double* d_db, int64_t lddb, double* d_da, int64_t ldda, int mode);
+/* Mixed-precision form: lambda by refinement on A^T (low-precision factors,
+ * FP64 residual; same options and statuses as luhot_dgesv_ir_dev), dA in FP64. */
+int luhot_dgesv_backward_ir_dev(luhot_ctx* ctx, int64_t n, int64_t nrhs, const double* d_a, int64_t lda,
+                                const double* d_x, int64_t ldx, const double* d_w, int64_t ldw,
+                                double* d_db, int64_t lddb, double* d_da, int64_t ldda, int precision,
+                                int solver, double tol, int max_iter, luhot_ir_info* info);
+
+/* ---- Batched uneven solves ----------------------------------------------
+ * No lair counterpart: lair factors one matrix per call; these factor and
+ * solve `count` independent systems A_i x_i = b_i (1 <= n_i <= 256) in one
+ * persistent kernel launch replayed from a CUDA graph, with lair's per-system
+ * semantics (pivots, last-zero-pivot singular step; LUHOT_MODE_EXACT gives
+ * lair's bits for every system).  Packed layout: A_i row-major at element
+ * offset sum_{j<i} n_j^2, b_i (overwritten by x_i) and int32 pivots at
+ * sum_{j<i} n_j, info[i] = singular step or -1.  dtype 0 = f64, 1 = f32. */
+typedef struct luhot_batch luhot_batch;
+int luhot_batch_create(luhot_ctx* ctx, int64_t count, const int32_t* sizes, int dtype, int mode,
+                       luhot_batch** out);
+void luhot_batch_destroy(luhot_batch* plan);
+/* Total elements of the packed A and b arrays. */
+int luhot_batch_layout(const luhot_batch* plan, int64_t* a_elems, int64_t* b_elems);
+/* Choose, per size bucket, the shared-memory path or a panel width (8, 16,
+ * 32) by timing each on sample systems copied from d_a / d_b (not modified). */
+int luhot_batch_autotune(luhot_batch* plan, const void* d_a, const void* d_b);
+/* Chosen per-bucket settings (9 buckets: 0 = shared memory, else the panel
+ * width) and the largest n of the shared-memory path. */
+int luhot_batch_tuning(const luhot_batch* plan, int32_t* nb_per_bucket, int32_t* smem_n);
+/* Factor and solve every system in place on the device (one graph launch). */
+int luhot_batch_solve(luhot_batch* plan, void* d_a, void* d_b, int32_t* d_piv, int32_t* d_info);
+/* Same with packed host arrays (copied in and out). */
+int luhot_batch_solve_host(luhot_batch* plan, void* a, void* b, int32_t* piv, int32_t* info);
+
 /* ---- Device-resident entry points ------------------------------------ */
 /* Matrices are row-major on the device with leading dimension ld (elements);
  * pivots are int32 on the device.  The call is asynchronous on the context's

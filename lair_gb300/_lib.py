@@ -58,6 +58,19 @@ SIGNATURES = {
     "luhot_dgesv_ir_dev": (_i32, [_vp, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _i32, _i32, _dbl, _i32, _vp]),
     "luhot_dgesv_ir": (_i32, [_vp, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _i32, _i32, _dbl,
                               _i32, _vp]),
+    "luhot_dgesv_backward": (_i32, [_vp, _i64, _i64, _vp, _i64, _i64, _vp, _vp, _i64, _i64, _vp, _i64, _i64, _vp,
+                                    _i64, _i64, _vp, _i64, _i64, _i32]),
+    "luhot_dgesv_backward_dev": (_i32, [_vp, _i64, _i64, _vp, _i64, _vp, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64,
+                                        _i32]),
+    "luhot_dgesv_backward_ir_dev": (_i32, [_vp, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64,
+                                           _i32, _i32, _dbl, _i32, _vp]),
+    "luhot_batch_create": (_i32, [_vp, _i64, _vp, _i32, _i32, ctypes.POINTER(_vp)]),
+    "luhot_batch_destroy": (None, [_vp]),
+    "luhot_batch_layout": (_i32, [_vp, _vp, _vp]),
+    "luhot_batch_autotune": (_i32, [_vp, _vp, _vp]),
+    "luhot_batch_tuning": (_i32, [_vp, _vp, _vp]),
+    "luhot_batch_solve": (_i32, [_vp, _vp, _vp, _vp, _vp]),
+    "luhot_batch_solve_host": (_i32, [_vp, _vp, _vp, _vp, _vp]),
     "luhot_dgetrs_dev_noalloc": (_i32, [_i64, _i64, _vp, _i64, _vp, _vp, _i64, _i32, _i32, _vp]),
 }
 

@@ -85,7 +85,7 @@ __global__ void transpose_kernel(const T* src, int64_t lds, T* dst, int64_t ldd,
 }
 
 template <typename T>
-static int launch_transpose(luhot_ctx* ctx, const T* src, int64_t lds, T* dst, int64_t ldd, int rows,
+int launch_transpose(luhot_ctx* ctx, const T* src, int64_t lds, T* dst, int64_t ldd, int rows,
                             int cols) {
   dim3 grid((cols + 31) / 32, (rows + 31) / 32), block(32, 8);
   transpose_kernel<T><<<grid, block, 0, ctx->stream>>>(src, lds, dst, ldd, rows, cols);
@@ -155,7 +155,7 @@ static Layout classify(int64_t m, int64_t n, int64_t rs, int64_t cs) {
 // Host (m x n, rs, cs) -> device row-major (ldd).  `tmp` is device scratch
 // of at least m*n elements for the F-order path.
 template <typename T>
-static int stage_in(luhot_ctx* ctx, const T* h, int64_t m, int64_t n, int64_t rs, int64_t cs, T* d,
+int stage_in(luhot_ctx* ctx, const T* h, int64_t m, int64_t n, int64_t rs, int64_t cs, T* d,
                     int64_t ldd, DevBuf& tmp) {
   if (m == 0 || n == 0) return LUHOT_OK;
   const Layout lay = classify(m, n, rs, cs);
@@ -194,7 +194,7 @@ static int stage_in(luhot_ctx* ctx, const T* h, int64_t m, int64_t n, int64_t rs
 
 // Device row-major (ldd) -> host (m x n, rs, cs).  Synchronises the stream.
 template <typename T>
-static int stage_out(luhot_ctx* ctx, const T* d, int64_t ldd, T* h, int64_t m, int64_t n, int64_t rs,
+int stage_out(luhot_ctx* ctx, const T* d, int64_t ldd, T* h, int64_t m, int64_t n, int64_t rs,
                      int64_t cs, DevBuf& tmp) {
   if (m == 0 || n == 0) return LUHOT_OK;
   const Layout lay = classify(m, n, rs, cs);
@@ -234,6 +234,14 @@ static int stage_out(luhot_ctx* ctx, const T* d, int64_t ldd, T* h, int64_t m, i
     for (int64_t j = 0; j < n; ++j) h[i * rs + j * cs] = packed[(size_t)i * n + j];
   return LUHOT_OK;
 }
+
+template int stage_in<double>(luhot_ctx*, const double*, int64_t, int64_t, int64_t, int64_t, double*, int64_t,
+                              DevBuf&);
+template int stage_in<float>(luhot_ctx*, const float*, int64_t, int64_t, int64_t, int64_t, float*, int64_t, DevBuf&);
+template int stage_out<double>(luhot_ctx*, const double*, int64_t, double*, int64_t, int64_t, int64_t, int64_t,
+                               DevBuf&);
+template int stage_out<float>(luhot_ctx*, const float*, int64_t, float*, int64_t, int64_t, int64_t, int64_t, DevBuf&);
+template int launch_transpose<double>(luhot_ctx*, const double*, int64_t, double*, int64_t, int, int);
 
 static bool dims_ok(int64_t m, int64_t n) {
   return m >= 0 && n >= 0 && m < (int64_t)INT32_MAX && n < (int64_t)INT32_MAX &&
@@ -321,14 +329,7 @@ static int getrs_host(luhot_ctx* ctx, int64_t n, int64_t nrhs, const T* lu, int6
 using namespace luhot;
 
 namespace {
-struct Guard {
-  explicit Guard(luhot_ctx* c) : ctx(c), lock(c->mu) {
-    cudaSetDevice(c->device);
-    ctx->last_error.clear();
-  }
-  luhot_ctx* ctx;
-  std::lock_guard<std::mutex> lock;
-};
+using Guard = luhot::CtxGuard;
 }  // namespace
 
 extern "C" {
@@ -397,6 +398,7 @@ void luhot_destroy(luhot_ctx* ctx) {
   if (ctx->h_scalars) cudaFreeHost(ctx->h_scalars);
   for (auto& b : ctx->ir_buf)
     if (b.ptr) cudaFree(b.ptr);
+  if (ctx->adj_buf.ptr) cudaFree(ctx->adj_buf.ptr);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
 }

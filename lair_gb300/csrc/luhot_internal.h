@@ -61,6 +61,7 @@ struct luhot_ctx {
   luhot::DevBuf perm_buf;                   // int32 permutation
   luhot::DevBuf trsv_buf;                   // ready flags + ticket of the triangular sweeps
   luhot::DevBuf ir_buf[4];                  // refinement: low-precision LU, vectors, indices, rhs
+  luhot::DevBuf adj_buf;                    // adjoint: A^T or dA
   double* h_scalars = nullptr;              // pinned: scalars read back by the refinement loop
   void* h_piv = nullptr;                    // pinned pivots staging
   size_t h_piv_bytes = 0;
@@ -107,6 +108,27 @@ int getrs_perm(luhot_ctx* ctx, const int* piv, int n, int* perm);
 template <typename T>
 int getrs_apply(luhot_ctx* ctx, int n, int nrhs, const T* lu, int64_t lda, const int* perm, const T* b,
                 int64_t ldb, T* x, int64_t ldx, int trans, int mode, T* w);
+
+// Held by every C entry point: serialises calls on a context, makes its
+// device current and clears the last error message.
+struct CtxGuard {
+  explicit CtxGuard(luhot_ctx* c) : ctx(c), lock(c->mu) {
+    cudaSetDevice(c->device);
+    ctx->last_error.clear();
+  }
+  luhot_ctx* ctx;
+  std::lock_guard<std::mutex> lock;
+};
+
+// Stage a host matrix (any strides) into / out of a row-major device buffer.
+template <typename T>
+int stage_in(luhot_ctx* ctx, const T* h, int64_t m, int64_t n, int64_t rs, int64_t cs, T* d, int64_t ldd, DevBuf& tmp);
+template <typename T>
+int stage_out(luhot_ctx* ctx, const T* d, int64_t ldd, T* h, int64_t m, int64_t n, int64_t rs, int64_t cs,
+              DevBuf& tmp);
+// dst (row-major, ldd) <- transpose of src (rows x cols, lds).
+template <typename T>
+int launch_transpose(luhot_ctx* ctx, const T* src, int64_t lds, T* dst, int64_t ldd, int rows, int cols);
 
 inline void count_launch(luhot_ctx* ctx, int64_t k = 1) { ctx->launches.fetch_add(k); }
 
