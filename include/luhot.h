@@ -133,9 +133,17 @@ int luhot_dgesv(luhot_ctx* ctx, int64_t n, int64_t nrhs, const double* a, int64_
  * LUHOT_REFINE_IR: d = (LU)^-1 r in the low precision (converges for
  * kappa * u_low < 1); LUHOT_REFINE_GMRES: d from FP64 GMRES preconditioned
  * by the low-precision LU (Carson & Higham), for larger kappa * u_low. */
+/* Factorization precisions.  FP32: FP32 LU on the CUDA cores.  BF16 / FP16:
+ * FP32 storage and panels, Schur updates on the tensor cores (tcgen05) with
+ * BF16 / FP16 operands scaled per panel by a power of two and FP32
+ * accumulation.  TF32: the same with FP32 operands read as TF32.  BF16X3:
+ * FP32-accurate Schur updates on the BF16 tensor cores, each FP32 operand
+ * split into three BF16 pieces and six piece products accumulated in FP32. */
 #define LUHOT_PREC_FP32 0
 #define LUHOT_PREC_BF16 1
 #define LUHOT_PREC_FP16 2
+#define LUHOT_PREC_TF32 3
+#define LUHOT_PREC_BF16X3 4
 #define LUHOT_REFINE_IR 0
 #define LUHOT_REFINE_GMRES 1
 

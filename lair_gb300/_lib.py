@@ -87,8 +87,8 @@ class Profile(ctypes.Structure):
                 for i, name in enumerate(PROFILE_CLASSES) if self.launches[i]}
 
 
-PREC_FP32, PREC_BF16, PREC_FP16 = 0, 1, 2
-PRECISIONS = {"fp32": PREC_FP32, "bf16": PREC_BF16, "fp16": PREC_FP16}
+PREC_FP32, PREC_BF16, PREC_FP16, PREC_TF32, PREC_BF16X3 = 0, 1, 2, 3, 4
+PRECISIONS = {"fp32": PREC_FP32, "bf16": PREC_BF16, "fp16": PREC_FP16, "tf32": PREC_TF32, "bf16x3": PREC_BF16X3}
 REFINE_IR, REFINE_GMRES = 0, 1
 SOLVERS = {"ir": REFINE_IR, "gmres": REFINE_GMRES}
 

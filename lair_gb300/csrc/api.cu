@@ -6,6 +6,7 @@
 // device routine runs, and the result is written back in the caller's own
 // layout, as lair's in-place getrf leaves it (src/lapack/getrf.rs:12-27).
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -363,6 +364,10 @@ int luhot_create(luhot_ctx** out, int device) {
   luhot_ctx* ctx = new (std::nothrow) luhot_ctx();
   if (!ctx) return LUHOT_ERR_ALLOC;
   ctx->device = device;
+  {
+    const char* tr = std::getenv("LUHOT_TRACE");
+    ctx->trace = tr && tr[0] == '1';
+  }
   cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
   cudaDeviceGetAttribute(&ctx->max_smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
   bool ok = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) == cudaSuccess;
@@ -399,6 +404,7 @@ void luhot_destroy(luhot_ctx* ctx) {
   for (auto& b : ctx->ir_buf)
     if (b.ptr) cudaFree(b.ptr);
   if (ctx->adj_buf.ptr) cudaFree(ctx->adj_buf.ptr);
+  if (ctx->tc_buf.ptr) cudaFree(ctx->tc_buf.ptr);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
 }
@@ -413,7 +419,7 @@ int luhot_set_stream(luhot_ctx* ctx, void* cuda_stream) {
 }
 
 int luhot_set_block(luhot_ctx* ctx, int nb) {
-  if (!ctx || nb < 0 || nb > kMaxPanelWidth) return LUHOT_ERR_INVALID_ARG;
+  if (!ctx || nb < 0 || nb > kDefaultPanelWidth) return LUHOT_ERR_INVALID_ARG;
   Guard g(ctx);
   ctx->nb_override = nb;
   return LUHOT_OK;

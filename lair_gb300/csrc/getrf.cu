@@ -28,6 +28,7 @@
 
 #include "common.cuh"
 #include "luhot_internal.h"
+#include "tc_gemm.cuh"
 
 namespace luhot {
 
@@ -524,7 +525,8 @@ static int launch_gemm(luhot_ctx* ctx, T* a, int64_t lda, int r0, int c0, int kk
 
 template <typename T, bool kExact>
 static int getrf_impl(luhot_ctx* ctx, int m, int n, T* a, int64_t lda, int* piv, int nb,
-                      cudaStream_t stream) {
+                      cudaStream_t stream, int tc_kind = -1, void* tc_a = nullptr, void* tc_b = nullptr,
+                      float* tc_scal = nullptr) {
   const int dim_min = std::min(m, n);
   unsigned int bar_count = 0;
   for (int k0 = 0; k0 < dim_min; k0 += nb) {
@@ -551,6 +553,13 @@ static int getrf_impl(luhot_ctx* ctx, int m, int n, T* a, int64_t lda, int* piv,
       prof_end(ctx, kProfTrsm, (double)w * (w - 1) * (n - c_right),
                ((double)w * w + 2.0 * w * (n - c_right)) * sizeof(T));
       LUHOT_CUDA_TRY(ctx, cudaGetLastError());
+      if constexpr (std::is_same<T, float>::value) {
+        if (tc_kind >= 0) {
+          rc = tc_schur_update(ctx, tc_kind, a, lda, k0, w, m, n, tc_a, tc_b, tc_scal, stream);
+          if (rc != LUHOT_OK) return rc;
+          continue;
+        }
+      }
       rc = launch_gemm<T, kExact>(ctx, a, lda, k0 + w, c_right, k0, w, m - (k0 + w), n - c_right,
                                   stream);
       if (rc != LUHOT_OK) return rc;
@@ -568,7 +577,7 @@ int getrf_device(luhot_ctx* ctx, int m, int n, T* a, int64_t lda, int* piv, int 
   cudaStream_t stream = ctx->stream;
   int rc = reset_status(ctx);
   if (rc != LUHOT_OK) return rc;
-  const int nb = ctx->nb_override > 0 ? std::min(ctx->nb_override, kMaxPanelWidth) : kMaxPanelWidth;
+  const int nb = ctx->nb_override > 0 ? std::min(ctx->nb_override, kDefaultPanelWidth) : kDefaultPanelWidth;
   if (mode == LUHOT_MODE_EXACT)
     rc = getrf_impl<T, true>(ctx, m, n, a, lda, piv, nb, stream);
   else
@@ -579,5 +588,24 @@ int getrf_device(luhot_ctx* ctx, int m, int n, T* a, int64_t lda, int* piv, int 
 
 template int getrf_device<double>(luhot_ctx*, int, int, double*, int64_t, int*, int, int64_t*);
 template int getrf_device<float>(luhot_ctx*, int, int, float*, int64_t, int*, int, int64_t*);
+
+int getrf_device_tc(luhot_ctx* ctx, int m, int n, float* a, int64_t lda, int* piv, int tc_kind, int64_t* singular) {
+  if (m < 0 || n < 0 || lda < std::max(1, n)) return set_error(ctx, LUHOT_ERR_INVALID_ARG, "getrf: bad shape or lda");
+  if (singular) *singular = -1;
+  if (m == 0 || n == 0) return LUHOT_OK;
+  const int nb = kTcPanelWidth;
+  const size_t bytes = tc_operand_bytes(tc_kind, m, nb) + tc_operand_bytes(tc_kind, n, nb) + 4096;
+  int rc = ensure_buf(ctx, ctx->tc_buf, bytes);
+  if (rc) return rc;
+  char* base = static_cast<char*>(ctx->tc_buf.ptr);
+  void* tc_a = base;
+  void* tc_b = base + (tc_operand_bytes(tc_kind, m, nb) + 1023) / 1024 * 1024;
+  float* tc_scal = reinterpret_cast<float*>(base + bytes - 1024);
+  rc = reset_status(ctx);
+  if (rc != LUHOT_OK) return rc;
+  rc = getrf_impl<float, false>(ctx, m, n, a, lda, piv, nb, ctx->stream, tc_kind, tc_a, tc_b, tc_scal);
+  if (rc != LUHOT_OK) return rc;
+  return finish_status(ctx, singular);
+}
 
 }  // namespace luhot

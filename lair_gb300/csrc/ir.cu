@@ -8,20 +8,25 @@
 // Converges when kappa(A) * u_low < 1 (FP32: kappa up to ~1e6).
 // GMRES-IR (Carson & Higham, SIAM J. Sci. Comput. 2017/2018): the correction
 // equation A d = r is solved by restarted GMRES in FP64 on the left-
-// preconditioned system (LU)^-1 A d = (LU)^-1 r, with the low-precision
-// factors applied in the low precision; classical Gram-Schmidt with one
-// reorthogonalisation pass; Givens rotations and the small least-squares
-// problem on the host.  It converges for much larger kappa * u_low.
+// preconditioned system (LU)^-1 A d = (LU)^-1 r; the low-precision factors
+// are applied to FP64 vectors in FP64 arithmetic (their storage stays FP32),
+// so each preconditioner application is accurate to the factors themselves;
+// classical Gram-Schmidt with one reorthogonalisation pass; Givens rotations
+// and the small least-squares problem on the host.  It converges for much
+// larger kappa * u_low.
 //
-// Every low-precision solve scales its right-hand side by its infinity norm
-// first (the scale stays on the device), so tiny residuals neither underflow
-// nor lose relative accuracy in the low precision.
+// Every plain-IR correction solve scales its right-hand side by its
+// infinity norm first (the scale stays on the device), so tiny residuals
+// neither underflow nor lose relative accuracy in the low precision.
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <vector>
 
 #include "common.cuh"
 #include "luhot_internal.h"
+#include "tc_gemm.cuh"
+#include "trsv.cuh"
 
 namespace luhot {
 
@@ -94,6 +99,11 @@ __global__ void ir_matvec_kernel(const double* __restrict__ a, int64_t lda, cons
       r[warp] = s;
     }
   }
+}
+
+// out[i] = v[perm[i]] (P^T v).
+__global__ void ir_gather_kernel(const double* __restrict__ v, const int* __restrict__ perm, double* out, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = v[perm[i]];
 }
 
 __global__ void ir_infnorm_kernel(const double* __restrict__ v, int n, double* out) {
@@ -204,7 +214,7 @@ __global__ void ir_combine_kernel(const double* __restrict__ V, int k, const dou
 // ---------------------------------------------------------------------------
 namespace {
 
-constexpr int kGmresRestart = 40;
+constexpr int kGmresRestart = 120;
 constexpr double kGmresTol = 1e-6;  // relative reduction of the preconditioned residual per solve
 
 // Device scalars.
@@ -248,6 +258,29 @@ struct IrRun {
   }
 
   // out (FP64) = (LU)^-1 v, through the low precision with infinity-norm scaling.
+  // out (FP64) = (LU)^-1 v with the low-precision factors applied in FP64
+  // arithmetic on FP64 vectors (no rounding of the Krylov vectors): the
+  // preconditioner of GMRES-IR, whose accuracy then depends only on the
+  // factors, not on u_low * kappa of each application.
+  int lo_solve64(const double* v, double* out) {
+    int* flags = nullptr;
+    int* ticket = nullptr;
+    int rc = trsv_scratch(ctx, n, &flags, &ticket);
+    if (rc) return rc;
+    prof_begin(ctx, kProfRefine);
+    ir_gather_kernel<<<grid_vec, 256, 0, ctx->stream>>>(v, perm, out, n);
+    prof_end(ctx, kProfRefine, 0.0, 20.0 * n);
+    prof_begin(ctx, kProfTrsv);
+    cudaError_t e = launch_trsv_syncfree<double, Tlo>(ctx->stream, lu, ldlo, out, 1, n, 1, true, true, false, false,
+                                                      flags, ticket, ctx->d_status);
+    if (e == cudaSuccess)
+      e = launch_trsv_syncfree<double, Tlo>(ctx->stream, lu, ldlo, out, 1, n, 1, false, false, false, false, flags,
+                                            ticket, ctx->d_status);
+    prof_end(ctx, kProfTrsv, 2.0 * n * (double)n, (double)n * n * sizeof(Tlo) + 32.0 * n);
+    if (e != cudaSuccess) return set_error(ctx, LUHOT_ERR_CUDA, std::string("ir sweep: ") + cudaGetErrorString(e));
+    return LUHOT_OK;
+  }
+
   int lo_solve(const double* v, double* out, bool add_into_out) {
     int rc = zero_scalar(kVscale);
     if (rc) return rc;
@@ -294,7 +327,7 @@ struct IrRun {
   int gmres_cycle(double* x, int* inner) {
     const int m = kGmresRestart;
     // v0 = M^-1 r / ||M^-1 r||_2
-    int rc = lo_solve(r, t, false);
+    int rc = lo_solve64(r, t);
     if (rc) return rc;
     rc = zero_scalar(kNrm2);
     if (rc) return rc;
@@ -316,7 +349,7 @@ struct IrRun {
       double* vk1 = V + (int64_t)(k + 1) * n;
       rc = matvec(vk, r);  // r is free as scratch inside the cycle
       if (rc) return rc;
-      rc = lo_solve(r, vk1, false);
+      rc = lo_solve64(r, vk1);
       if (rc) return rc;
       // Two passes of classical Gram-Schmidt against v_0..v_k.
       std::vector<double> hcol(k + 2, 0.0);
@@ -378,31 +411,28 @@ struct IrRun {
 
 }  // namespace
 
-template <typename Tlo>
-static int gesv_ir_impl(luhot_ctx* ctx, int n, const double* a, int64_t lda, const double* b, double* x,
-                        int solver, double tol, int max_iter, luhot_ir_info* info) {
-  cudaStream_t stream = ctx->stream;
+// Refinement state shared by every right-hand side of one call.
+static int ir_setup(luhot_ctx* ctx, int n, const double* a, int64_t lda, IrRun<float>& s) {
   const int64_t ldlo = ((int64_t)n + 63) / 64 * 64;
-  int rc = ensure_buf(ctx, ctx->ir_buf[0], (size_t)n * ldlo * sizeof(Tlo));
+  int rc = ensure_buf(ctx, ctx->ir_buf[0], (size_t)n * ldlo * sizeof(float));
   if (rc) return rc;
   const size_t vecs = (size_t)n * sizeof(double);
-  rc = ensure_buf(ctx, ctx->ir_buf[1], vecs * (2 + kGmresRestart + 1) + 3 * (size_t)n * sizeof(Tlo) + 4096);
+  rc = ensure_buf(ctx, ctx->ir_buf[1], vecs * (2 + kGmresRestart + 1) + 3 * (size_t)n * sizeof(float) + 4096);
   if (rc) return rc;
   const size_t idx_ints = (2 * (size_t)n + 63) / 64 * 64;  // pivots + permutation, 256-byte aligned end
   rc = ensure_buf(ctx, ctx->ir_buf[2], idx_ints * sizeof(int) + 256 * sizeof(double));
   if (rc) return rc;
-  IrRun<Tlo> s;
   s.ctx = ctx;
   s.n = n;
   s.a = a;
   s.lda = lda;
-  s.lu = static_cast<Tlo*>(ctx->ir_buf[0].ptr);
+  s.lu = static_cast<float*>(ctx->ir_buf[0].ptr);
   s.ldlo = ldlo;
   char* base = static_cast<char*>(ctx->ir_buf[1].ptr);
   s.r = reinterpret_cast<double*>(base);
   s.t = s.r + n;
   s.V = s.t + n;
-  s.lo1 = reinterpret_cast<Tlo*>(s.V + (size_t)(kGmresRestart + 1) * n);
+  s.lo1 = reinterpret_cast<float*>(s.V + (size_t)(kGmresRestart + 1) * n);
   s.lo2 = s.lo1 + n;
   s.low = s.lo2 + n;
   s.piv = static_cast<int*>(ctx->ir_buf[2].ptr);
@@ -410,45 +440,50 @@ static int gesv_ir_impl(luhot_ctx* ctx, int n, const double* a, int64_t lda, con
   s.sc = reinterpret_cast<double*>(s.piv + idx_ints);
   s.hsc = ctx->h_scalars;
   s.grid_vec = std::min(ctx->num_sms * 4, (n + 255) / 256);
+  return LUHOT_OK;
+}
 
-  cudaEvent_t e0, e1, e2;
-  cudaEventCreate(&e0);
-  cudaEventCreate(&e1);
-  cudaEventCreate(&e2);
-  struct EvGuard {
-    cudaEvent_t a, b, c;
-    ~EvGuard() {
-      cudaEventDestroy(a);
-      cudaEventDestroy(b);
-      cudaEventDestroy(c);
-    }
-  } guard{e0, e1, e2};
-  cudaEventRecord(e0, stream);
-
-  // 1. FP64 -> low precision, ||A||_inf.
-  LUHOT_CUDA_TRY(ctx, cudaMemsetAsync(s.sc, 0, 64 * sizeof(double), stream));
+// FP64 -> FP32 copy with ||A||_inf, then the low-precision LU: FP32 on the
+// CUDA cores, or FP32 storage with tensor-core Schur updates (TF32, or BF16 /
+// FP16 operands with per-panel scaling).
+static int ir_factor(IrRun<float>& s, int precision, luhot_ir_info* info) {
+  luhot_ctx* ctx = s.ctx;
+  const int n = s.n;
+  LUHOT_CUDA_TRY(ctx, cudaMemsetAsync(s.sc, 0, 64 * sizeof(double), ctx->stream));
   prof_begin(ctx, kProfRefine);
-  ir_convert_kernel<Tlo><<<(n + 7) / 8, 256, 0, stream>>>(a, lda, s.lu, ldlo, n, s.sc + kAnorm);
-  prof_end(ctx, kProfRefine, (double)n * n, (8.0 + sizeof(Tlo)) * n * (double)n);
-  rc = s.launch_check("ir convert");
+  ir_convert_kernel<float><<<(n + 7) / 8, 256, 0, ctx->stream>>>(s.a, s.lda, s.lu, s.ldlo, n, s.sc + kAnorm);
+  prof_end(ctx, kProfRefine, (double)n * n, 12.0 * n * (double)n);
+  int rc = s.launch_check("ir convert");
   if (rc) return rc;
-  // 2. Low-precision LU.
   int64_t sing = -1;
-  rc = getrf_device<Tlo>(ctx, n, n, s.lu, ldlo, s.piv, LUHOT_MODE_FAST, &sing);
+  if (precision == LUHOT_PREC_FP32) {
+    rc = getrf_device<float>(ctx, n, n, s.lu, s.ldlo, s.piv, LUHOT_MODE_FAST, &sing);
+  } else {
+    const int kind = precision == LUHOT_PREC_BF16     ? kTcBF16
+                     : precision == LUHOT_PREC_FP16   ? kTcFP16
+                     : precision == LUHOT_PREC_BF16X3 ? kTcBF16x3
+                                                      : kTcTF32;
+    rc = getrf_device_tc(ctx, n, n, s.lu, s.ldlo, s.piv, kind, &sing);
+  }
   if (rc) return rc;
   info->singular = sing;
   if (sing >= 0) return set_error(ctx, LUHOT_ERR_SINGULAR, "the low-precision factor is singular");
-  rc = getrs_perm(ctx, s.piv, n, s.perm);
-  if (rc) return rc;
-  cudaEventRecord(e1, stream);
+  return getrs_perm(ctx, s.piv, n, s.perm);
+}
 
-  // 3. ||b||_inf and the first solve x0 = (LU)^-1 b.
+// Refine one right-hand side (contiguous b, x) with the factors in s.
+static int ir_refine(IrRun<float>& s, const double* b, double* x, int solver, double tol, int max_iter,
+                     luhot_ir_info* info) {
+  luhot_ctx* ctx = s.ctx;
+  cudaStream_t stream = ctx->stream;
+  const int n = s.n;
+  int rc = s.zero_scalar(kBnorm);
+  if (rc) return rc;
   prof_begin(ctx, kProfRefine);
   ir_infnorm_kernel<<<s.grid_vec, 256, 0, stream>>>(b, n, s.sc + kBnorm);
   prof_end(ctx, kProfRefine, 0.0, 8.0 * n);
   rc = s.lo_solve(b, x, false);
   if (rc) return rc;
-
   const double tol_eff = tol > 0.0 ? tol : n * std::ldexp(1.0, -53);
   int it = 0, inner_total = 0;
   double berr = INFINITY, prev = INFINITY;
@@ -467,6 +502,7 @@ static int gesv_ir_impl(luhot_ctx* ctx, int n, const double* a, int64_t lda, con
     const double anorm = s.hsc[kAnorm], bnorm = s.hsc[kBnorm], rnorm = s.hsc[kRnorm], xnorm = s.hsc[kXnorm];
     berr = rnorm / (anorm * xnorm + bnorm);
     if (!std::isfinite(berr)) berr = INFINITY;
+    if (ctx->trace) fprintf(stderr, "luhot ir: step %d berr %.3e inner %d\n", it, berr, inner_total);
     if (berr <= tol_eff) {
       converged = true;
       break;
@@ -475,7 +511,7 @@ static int gesv_ir_impl(luhot_ctx* ctx, int n, const double* a, int64_t lda, con
     // Stop when the iteration no longer contracts (plain IR diverging, or
     // stagnation at the attainable accuracy).
     if (berr > 0.9 * prev) {
-      if (++stall >= 2) break;
+      if (++stall >= 3) break;
     } else {
       stall = 0;
     }
@@ -491,16 +527,9 @@ static int gesv_ir_impl(luhot_ctx* ctx, int n, const double* a, int64_t lda, con
     }
     ++it;
   }
-  cudaEventRecord(e2, stream);
-  LUHOT_CUDA_TRY(ctx, cudaEventSynchronize(e2));
-  float f_ms = 0.f, r_ms = 0.f;
-  cudaEventElapsedTime(&f_ms, e0, e1);
-  cudaEventElapsedTime(&r_ms, e1, e2);
   info->iterations = std::max(info->iterations, it);
   info->inner_iterations += inner_total;
   info->backward_error = std::max(info->backward_error, berr);
-  info->factor_ms += f_ms;
-  info->refine_ms += r_ms;
   info->converged = info->converged && converged;
   return LUHOT_OK;
 }
@@ -512,6 +541,9 @@ int gesv_ir_device(luhot_ctx* ctx, int n, int nrhs, const double* a, int64_t lda
     return set_error(ctx, LUHOT_ERR_INVALID_ARG, "gesv_ir: bad shape or leading dimension");
   if (solver != LUHOT_REFINE_IR && solver != LUHOT_REFINE_GMRES)
     return set_error(ctx, LUHOT_ERR_INVALID_ARG, "gesv_ir: unknown solver");
+  if (precision != LUHOT_PREC_FP32 && precision != LUHOT_PREC_BF16 && precision != LUHOT_PREC_FP16 &&
+      precision != LUHOT_PREC_TF32 && precision != LUHOT_PREC_BF16X3)
+    return set_error(ctx, LUHOT_ERR_INVALID_ARG, "gesv_ir: unknown precision");
   if (max_iter < 0) return set_error(ctx, LUHOT_ERR_INVALID_ARG, "gesv_ir: negative max_iter");
   *info = luhot_ir_info{};
   info->converged = 1;
@@ -519,29 +551,47 @@ int gesv_ir_device(luhot_ctx* ctx, int n, int nrhs, const double* a, int64_t lda
   info->solver = solver;
   info->singular = -1;
   if (n == 0 || nrhs == 0) return LUHOT_OK;
-  if (precision != LUHOT_PREC_FP32)
-    return set_error(ctx, LUHOT_ERR_UNSUPPORTED, "gesv_ir: only the FP32 factorization is built");
   int rc = reset_status(ctx);
   if (rc) return rc;
-  // Columns of b and x are strided (ld); the driver works on contiguous vectors.
+  // Columns of b and x are strided (ld); the refinement works on contiguous vectors.
   rc = ensure_buf(ctx, ctx->ir_buf[3], (size_t)n * 2 * sizeof(double));
   if (rc) return rc;
   double* bc = static_cast<double*>(ctx->ir_buf[3].ptr);
   double* xc = bc + n;
+  IrRun<float> s;
+  rc = ir_setup(ctx, n, a, lda, s);
+  if (rc) return rc;
+  cudaEvent_t e0, e1, e2;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventCreate(&e2);
+  struct EvGuard {
+    cudaEvent_t a, b, c;
+    ~EvGuard() {
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+      cudaEventDestroy(c);
+    }
+  } guard{e0, e1, e2};
+  cudaEventRecord(e0, ctx->stream);
+  rc = ir_factor(s, precision, info);
+  if (rc) return rc;
+  cudaEventRecord(e1, ctx->stream);
   for (int c = 0; c < nrhs; ++c) {
-    {
-      int rc_ = copy_2d(ctx, bc, sizeof(double), b + c, ldb * sizeof(double), sizeof(double), n,
-                                          cudaMemcpyDeviceToDevice);
-      if (rc_) return rc_;
-    }
-    rc = gesv_ir_impl<float>(ctx, n, a, lda, bc, xc, solver, tol, max_iter, info);
+    rc = copy_2d(ctx, bc, sizeof(double), b + c, ldb * sizeof(double), sizeof(double), n, cudaMemcpyDeviceToDevice);
     if (rc) return rc;
-    {
-      int rc_ = copy_2d(ctx, x + c, ldx * sizeof(double), xc, sizeof(double), sizeof(double), n,
-                                          cudaMemcpyDeviceToDevice);
-      if (rc_) return rc_;
-    }
+    rc = ir_refine(s, bc, xc, solver, tol, max_iter, info);
+    if (rc) return rc;
+    rc = copy_2d(ctx, x + c, ldx * sizeof(double), xc, sizeof(double), sizeof(double), n, cudaMemcpyDeviceToDevice);
+    if (rc) return rc;
   }
+  cudaEventRecord(e2, ctx->stream);
+  LUHOT_CUDA_TRY(ctx, cudaEventSynchronize(e2));
+  float f_ms = 0.f, r_ms = 0.f;
+  cudaEventElapsedTime(&f_ms, e0, e1);
+  cudaEventElapsedTime(&r_ms, e1, e2);
+  info->factor_ms = f_ms;
+  info->refine_ms = r_ms;
   rc = finish_status(ctx, nullptr);
   if (rc) return rc;
   if (!info->converged)

@@ -15,8 +15,10 @@ namespace luhot {
 
 struct DeviceStatus;
 
-constexpr int kMaxPanelCtas = 256;   // >= SM count
-constexpr int kMaxPanelWidth = 64;   // default and largest panel width
+constexpr int kMaxPanelCtas = 256;     // >= SM count
+constexpr int kDefaultPanelWidth = 64; // FP64 / FP32 CUDA-core and DMMA paths
+constexpr int kTcPanelWidth = 128;     // tensor-core (tcgen05) Schur-update path
+constexpr int kMaxPanelWidth = 128;    // sizes the panel kernel's scratch
 
 // Grow-only device buffer.
 struct DevBuf {
@@ -62,10 +64,12 @@ struct luhot_ctx {
   luhot::DevBuf trsv_buf;                   // ready flags + ticket of the triangular sweeps
   luhot::DevBuf ir_buf[4];                  // refinement: low-precision LU, vectors, indices, rhs
   luhot::DevBuf adj_buf;                    // adjoint: A^T or dA
+  luhot::DevBuf tc_buf;                     // tensor-core LU: operand copies + scales
   double* h_scalars = nullptr;              // pinned: scalars read back by the refinement loop
   void* h_piv = nullptr;                    // pinned pivots staging
   size_t h_piv_bytes = 0;
   int nb_override = 0;
+  bool trace = false;  // LUHOT_TRACE=1: refinement steps are reported on stderr
   unsigned long long wait_timeout_ns = 2000000000ull;  // per device-side wait
   std::atomic<int64_t> launches{0};
   // CUDA-event profile (off by default): one event pair per launch.
@@ -93,6 +97,10 @@ int getrf_device(luhot_ctx* ctx, int m, int n, T* a, int64_t lda, int* piv, int 
 
 // Solve with device factors: X (n x nrhs, ldx) <- op(A)^-1 B.  b and x may be
 // the same buffer.
+// FP32 LU whose Schur updates run on the tensor cores (tcgen05) with
+// BF16 / FP16 / TF32 operands (TcKind) and FP32 accumulation; panel width 128.
+int getrf_device_tc(luhot_ctx* ctx, int m, int n, float* a, int64_t lda, int* piv, int tc_kind, int64_t* singular);
+
 int gesv_ir_device(luhot_ctx* ctx, int n, int nrhs, const double* a, int64_t lda, const double* b, int64_t ldb,
                    double* x, int64_t ldx, int precision, int solver, double tol, int max_iter,
                    luhot_ir_info* info);
@@ -105,6 +113,8 @@ int getrs_device(luhot_ctx* ctx, int n, int nrhs, const T* lu, int64_t lda, cons
 // (getrs_perm), then apply any number of solves with it (getrs_apply, async;
 // w is n x nrhs scratch that must not alias b or x).
 int getrs_perm(luhot_ctx* ctx, const int* piv, int n, int* perm);
+// Ready flags and ticket of the sync-free triangular sweeps for order n.
+int trsv_scratch(luhot_ctx* ctx, int n, int** flags, int** ticket);
 template <typename T>
 int getrs_apply(luhot_ctx* ctx, int n, int nrhs, const T* lu, int64_t lda, const int* perm, const T* b,
                 int64_t ldb, T* x, int64_t ldx, int trans, int mode, T* w);

@@ -48,9 +48,11 @@ __device__ __forceinline__ float tsub(float c, float l, float u) {
   return fmaf(-l, u, c);
 }
 
-template <typename T, bool kTrans>
-__device__ __forceinline__ T op_elem(const T* a, int64_t lda, int i, int k) {
-  return kTrans ? a[(int64_t)k * lda + i] : a[(int64_t)i * lda + k];
+// Element (i, k) of op(A), widened from the storage type TA to the
+// arithmetic type T (FP32 factors can be applied in FP64 arithmetic).
+template <typename T, typename TA, bool kTrans>
+__device__ __forceinline__ T op_elem(const TA* a, int64_t lda, int i, int k) {
+  return static_cast<T>(kTrans ? a[(int64_t)k * lda + i] : a[(int64_t)i * lda + k]);
 }
 
 // Element e of this thread's share of tile op(A)(i0.., k0..): (r, c) within
@@ -67,14 +69,14 @@ __device__ __forceinline__ void tile_coord(int e, int& r, int& c) {
   }
 }
 
-template <typename T, bool kTrans>
-__device__ __forceinline__ void tile_load(T (&reg)[kPrefetch], const T* a, int64_t lda, int i0, int k0, int rows,
+template <typename T, typename TA, bool kTrans>
+__device__ __forceinline__ void tile_load(T (&reg)[kPrefetch], const TA* a, int64_t lda, int i0, int k0, int rows,
                                           int cols) {
 #pragma unroll
   for (int e = 0; e < kPrefetch; ++e) {
     int r, c;
     tile_coord<kTrans>(e, r, c);
-    reg[e] = (r < rows && c < cols) ? op_elem<T, kTrans>(a, lda, i0 + r, k0 + c) : T(0);
+    reg[e] = (r < rows && c < cols) ? op_elem<T, TA, kTrans>(a, lda, i0 + r, k0 + c) : T(0);
   }
 }
 
@@ -129,8 +131,8 @@ __device__ __forceinline__ bool wait_ready(const int* flags, int j, DeviceStatus
 }
 
 // kNR: right-hand sides handled per launch (1, 2, 4 or 16; runtime nrhs <= kNR).
-template <typename T, bool kExact, bool kLower, bool kUnit, bool kTrans, int kNR>
-__global__ void __launch_bounds__(kThreads) trsv_syncfree_kernel(const T* __restrict__ a, int64_t lda, T* x,
+template <typename T, typename TA, bool kExact, bool kLower, bool kUnit, bool kTrans, int kNR>
+__global__ void __launch_bounds__(kThreads) trsv_syncfree_kernel(const TA* __restrict__ a, int64_t lda, T* x,
                                                                  int64_t ldx, int n, int nrhs, int* flags,
                                                                  int* ticket, DeviceStatus* st) {
   // Threads per (row, rhs) pair: k split only in fast mode.
@@ -176,7 +178,7 @@ __global__ void __launch_bounds__(kThreads) trsv_syncfree_kernel(const T* __rest
   T reg[kPrefetch];
   if (nupd > 0) {
     const int J0 = kLower ? 0 : nblk - 1;
-    tile_load<T, kTrans>(reg, a, lda, i0, J0 * kBS, rows, min(kBS, n - J0 * kBS));
+    tile_load<T, TA, kTrans>(reg, a, lda, i0, J0 * kBS, rows, min(kBS, n - J0 * kBS));
   }
   for (int s = 0; s < nupd; ++s) {
     const int J = kLower ? s : (nblk - 1 - s);
@@ -186,7 +188,7 @@ __global__ void __launch_bounds__(kThreads) trsv_syncfree_kernel(const T* __rest
     tile_store<T, kTrans>(tile, reg);
     if (s + 1 < nupd) {  // prefetch the next tile while this one is used
       const int Jn = kLower ? s + 1 : (nblk - 2 - s);
-      tile_load<T, kTrans>(reg, a, lda, i0, Jn * kBS, rows, min(kBS, n - Jn * kBS));
+      tile_load<T, TA, kTrans>(reg, a, lda, i0, Jn * kBS, rows, min(kBS, n - Jn * kBS));
     }
     if (!wait_ready(flags, J, st)) return;
     for (int idx = threadIdx.x; idx < kBS * kNR; idx += kThreads) {
@@ -220,7 +222,7 @@ __global__ void __launch_bounds__(kThreads) trsv_syncfree_kernel(const T* __rest
   T* diag = tile0;
   {
     T dreg[kPrefetch];
-    tile_load<T, kTrans>(dreg, a, lda, i0, i0, rows, rows);
+    tile_load<T, TA, kTrans>(dreg, a, lda, i0, i0, rows, rows);
     for (int idx = threadIdx.x; idx < kBS * kNR; idx += kThreads) xacc[idx] = T(0);
     __syncthreads();
     tile_store<T, kTrans>(diag, dreg);
@@ -301,15 +303,15 @@ __global__ void __launch_bounds__(kThreads) trsv_syncfree_kernel(const T* __rest
 size_t trsv_syncfree_smem(size_t elem) { return (2 * (size_t)kBS * kLds + 2 * (size_t)kBS * kMaxRhs) * elem; }
 int trsv_syncfree_blocks(int n) { return (n + kBS - 1) / kBS; }
 
-template <typename T, bool EX, bool LO, bool UN, bool TR>
-static cudaError_t launch_case(cudaStream_t stream, const T* a, int64_t lda, T* x, int64_t ldx, int n, int nc,
+template <typename T, typename TA, bool EX, bool LO, bool UN, bool TR>
+static cudaError_t launch_case(cudaStream_t stream, const TA* a, int64_t lda, T* x, int64_t ldx, int n, int nc,
                                int* flags, int* ticket, DeviceStatus* st) {
   const int nblk = trsv_syncfree_blocks(n);
   const size_t smem = trsv_syncfree_smem(sizeof(T));
   cudaError_t e;
 #define LUHOT_TRSV_NR(NR)                                                                       \
   {                                                                                             \
-    auto k = trsv_syncfree_kernel<T, EX, LO, UN, TR, NR>;                                       \
+    auto k = trsv_syncfree_kernel<T, TA, EX, LO, UN, TR, NR>;                                       \
     e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);        \
     if (e != cudaSuccess) return e;                                                             \
     k<<<nblk, kThreads, smem, stream>>>(a, lda, x, ldx, n, nc, flags, ticket, st);              \
@@ -322,8 +324,8 @@ static cudaError_t launch_case(cudaStream_t stream, const T* a, int64_t lda, T* 
 #undef LUHOT_TRSV_NR
 }
 
-template <typename T>
-cudaError_t launch_trsv_syncfree(cudaStream_t stream, const T* a, int64_t lda, T* x, int64_t ldx, int n, int nrhs,
+template <typename T, typename TA>
+cudaError_t launch_trsv_syncfree(cudaStream_t stream, const TA* a, int64_t lda, T* x, int64_t ldx, int n, int nrhs,
                                  bool lower, bool unit, bool trans, bool exact, int* flags, int* ticket,
                                  DeviceStatus* st) {
   if (n <= 0 || nrhs <= 0) return cudaSuccess;
@@ -335,15 +337,15 @@ cudaError_t launch_trsv_syncfree(cudaStream_t stream, const T* a, int64_t lda, T
     if (e != cudaSuccess) return e;
     T* xc = x + c0;
     if (exact && lower && unit && !trans)
-      e = launch_case<T, true, true, true, false>(stream, a, lda, xc, ldx, n, nc, flags, ticket, st);
+      e = launch_case<T, TA, true, true, true, false>(stream, a, lda, xc, ldx, n, nc, flags, ticket, st);
     else if (!exact && lower && unit && !trans)
-      e = launch_case<T, false, true, true, false>(stream, a, lda, xc, ldx, n, nc, flags, ticket, st);
+      e = launch_case<T, TA, false, true, true, false>(stream, a, lda, xc, ldx, n, nc, flags, ticket, st);
     else if (!exact && !lower && !unit && !trans)
-      e = launch_case<T, false, false, false, false>(stream, a, lda, xc, ldx, n, nc, flags, ticket, st);
+      e = launch_case<T, TA, false, false, false, false>(stream, a, lda, xc, ldx, n, nc, flags, ticket, st);
     else if (!exact && lower && !unit && trans)
-      e = launch_case<T, false, true, false, true>(stream, a, lda, xc, ldx, n, nc, flags, ticket, st);
+      e = launch_case<T, TA, false, true, false, true>(stream, a, lda, xc, ldx, n, nc, flags, ticket, st);
     else if (!exact && !lower && unit && trans)
-      e = launch_case<T, false, false, true, true>(stream, a, lda, xc, ldx, n, nc, flags, ticket, st);
+      e = launch_case<T, TA, false, false, true, true>(stream, a, lda, xc, ldx, n, nc, flags, ticket, st);
     else
       return cudaErrorNotSupported;
     if (e != cudaSuccess) return e;
@@ -351,6 +353,9 @@ cudaError_t launch_trsv_syncfree(cudaStream_t stream, const T* a, int64_t lda, T
   return cudaSuccess;
 }
 
+template cudaError_t launch_trsv_syncfree<double, float>(cudaStream_t, const float*, int64_t, double*, int64_t,
+                                                         int, int, bool, bool, bool, bool, int*, int*,
+                                                         DeviceStatus*);
 template cudaError_t launch_trsv_syncfree<double>(cudaStream_t, const double*, int64_t, double*, int64_t, int, int,
                                                   bool, bool, bool, bool, int*, int*, DeviceStatus*);
 template cudaError_t launch_trsv_syncfree<float>(cudaStream_t, const float*, int64_t, float*, int64_t, int, int,

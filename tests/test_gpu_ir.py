@@ -49,6 +49,54 @@ def test_fp32_refinement_reaches_fp64_backward_error(kappa, solver):
         assert info["inner_iterations"] >= info["iterations"]
 
 
+@pytest.mark.parametrize("precision", ["tf32", "bf16", "fp16"])
+def test_tensor_core_factor_is_a_valid_preconditioner(precision):
+    """One low-precision solve (no refinement) already has the backward error
+    of the operand precision (tf32/fp16 ~ 2^-11, bf16 ~ 2^-8); a broken
+    tcgen05 Schur update would give O(1)."""
+    n = 1000  # not a multiple of the 128-wide panels or tiles
+    a = conditioned(n, 1e2, 11)
+    b = np.random.default_rng(12).standard_normal(n)
+    x, info = refine.gesv_ir(a, b, precision=precision, solver="ir", max_iter=0, raise_on_failure=False)
+    assert berr(a, x, b) <= {"tf32": 5e-3, "fp16": 5e-3, "bf16": 5e-2}[precision]
+
+
+@pytest.mark.parametrize("precision,kappa", [("tf32", 1e4), ("fp16", 1e4), ("bf16", 1e2)])
+def test_tensor_core_gmres_ir_reaches_fp64_backward_error(precision, kappa):
+    # With 11-bit (tf32, fp16) or 8-bit (bf16) factors, kappa * u_low must stay
+    # well below ~1e3 for restarted GMRES to contract; kappa = 1e6 is left to
+    # the FP32-accurate factorizations.
+    n = 2048
+    a = conditioned(n, kappa, 13)
+    b = np.random.default_rng(14).standard_normal(n)
+    x, info = refine.gesv_ir(a, b, precision=precision, solver="gmres", max_iter=30)
+    assert info["converged"] == 1
+    assert berr(a, x, b) <= n * EPS64
+
+
+@pytest.mark.parametrize("kappa", [1e2, 1e4, 1e6])
+def test_bf16x3_tensor_core_factor_with_plain_ir(kappa):
+    """The three-piece BF16 Schur update is FP32-accurate, so plain IR
+    converges where the FP32 LU does (kappa up to ~1e6)."""
+    n = 2048
+    a = conditioned(n, kappa, 17)
+    b = np.random.default_rng(18).standard_normal(n)
+    x, info = refine.gesv_ir(a, b, precision="bf16x3", solver="ir")
+    assert info["converged"] == 1 and berr(a, x, b) <= n * EPS64
+    x1, _ = refine.gesv_ir(a, b, precision="bf16x3", solver="ir", max_iter=0, raise_on_failure=False)
+    x2, _ = refine.gesv_ir(a, b, precision="fp32", solver="ir", max_iter=0, raise_on_failure=False)
+    # one solve with the tensor-core factors is as good as with the FFMA FP32 factors
+    assert berr(a, x1, b) <= 4 * berr(a, x2, b) + 1e-12
+
+
+def test_tensor_core_plain_ir_small_kappa():
+    n = 1536
+    a = conditioned(n, 1e2, 15)
+    b = np.random.default_rng(16).standard_normal(n)
+    x, info = refine.gesv_ir(a, b, precision="tf32", solver="ir")
+    assert info["converged"] == 1 and berr(a, x, b) <= n * EPS64
+
+
 def test_refinement_multiple_rhs_and_strides():
     n = 600
     a = conditioned(n, 1e3, 3)
