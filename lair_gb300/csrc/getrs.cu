@@ -230,7 +230,7 @@ int trsv_scratch(luhot_ctx* ctx, int n, int** flags, int** ticket) {
 
 template <typename T>
 int getrs_apply(luhot_ctx* ctx, int n, int nrhs, const T* lu, int64_t lda, const int* perm, const T* b,
-                int64_t ldb, T* x, int64_t ldx, int trans, int mode, T* w) {
+                int64_t ldb, T* x, int64_t ldx, int trans, int mode, T* w, const T* dinv_l, const T* dinv_u) {
   cudaStream_t stream = ctx->stream;
   int* flags = nullptr;
   int* ticket = nullptr;
@@ -244,8 +244,9 @@ int getrs_apply(luhot_ctx* ctx, int n, int nrhs, const T* lu, int64_t lda, const
   // 16 right-hand sides).
   auto sweep = [&](bool lower, bool unit, bool tr, bool ex) -> int {
     prof_begin(ctx, kProfTrsv);
+    const T* dinv = (ex || tr) ? nullptr : (lower ? dinv_l : dinv_u);
     cudaError_t e = launch_trsv_syncfree<T>(stream, lu, lda, w, ldw, n, nrhs, lower, unit, tr, ex, flags, ticket,
-                                            ctx->d_status);
+                                            ctx->d_status, dinv);
     prof_end(ctx, kProfTrsv, (double)n * n * nrhs, ((double)n * n / 2 + 2.0 * total) * sizeof(T));
     if (e != cudaSuccess) return set_error(ctx, LUHOT_ERR_CUDA, std::string("getrs sweep: ") + cudaGetErrorString(e));
     return LUHOT_OK;
@@ -309,15 +310,44 @@ int getrs_device(luhot_ctx* ctx, int n, int nrhs, const T* lu, int64_t lda, cons
   // Work in a private buffer so that x may alias b.
   rc = ensure_buf(ctx, ctx->work[3], (size_t)n * nrhs * sizeof(T));
   if (rc) return rc;
-  rc = getrs_apply<T>(ctx, n, nrhs, lu, lda, perm, b, ldb, x, ldx, trans, mode, static_cast<T*>(ctx->work[3].ptr));
+  // Fast untransposed solves use the inverses of the diagonal blocks; one
+  // small launch (64 threads per block) against two n^2 sweeps.
+  T* dinv_l = nullptr;
+  T* dinv_u = nullptr;
+  if (!trans && mode == LUHOT_MODE_FAST) {
+    const size_t ne = trsv_inverse_elems(n);
+    rc = ensure_buf(ctx, ctx->dinv_buf, 2 * ne * sizeof(T));
+    if (rc) return rc;
+    dinv_l = static_cast<T*>(ctx->dinv_buf.ptr);
+    dinv_u = dinv_l + ne;
+    rc = invert_diag_blocks<T, T>(ctx, n, lu, lda, dinv_l, dinv_u);
+    if (rc) return rc;
+  }
+  rc = getrs_apply<T>(ctx, n, nrhs, lu, lda, perm, b, ldb, x, ldx, trans, mode, static_cast<T*>(ctx->work[3].ptr),
+                      dinv_l, dinv_u);
   if (rc) return rc;
   return finish_status(ctx, nullptr);
 }
 
+template <typename T, typename TA>
+int invert_diag_blocks(luhot_ctx* ctx, int n, const TA* lu, int64_t lda, T* dinv_l, T* dinv_u) {
+  prof_begin(ctx, kProfTrsv);
+  cudaError_t e = launch_trsv_invert_diag<T, TA>(ctx->stream, lu, lda, n, true, dinv_l);
+  if (e == cudaSuccess) e = launch_trsv_invert_diag<T, TA>(ctx->stream, lu, lda, n, false, dinv_u);
+  prof_end(ctx, kProfTrsv, 2.0 * 64.0 * 64.0 * 64.0 / 3.0 * ((n + 63) / 64),
+           4.0 * (double)trsv_inverse_elems(n) * sizeof(T));
+  count_launch(ctx);
+  if (e != cudaSuccess) return set_error(ctx, LUHOT_ERR_CUDA, std::string("diagonal inverses: ") + cudaGetErrorString(e));
+  return LUHOT_OK;
+}
+
 template int getrs_apply<double>(luhot_ctx*, int, int, const double*, int64_t, const int*, const double*, int64_t,
-                                 double*, int64_t, int, int, double*);
+                                 double*, int64_t, int, int, double*, const double*, const double*);
 template int getrs_apply<float>(luhot_ctx*, int, int, const float*, int64_t, const int*, const float*, int64_t,
-                                float*, int64_t, int, int, float*);
+                                float*, int64_t, int, int, float*, const float*, const float*);
+template int invert_diag_blocks<double, double>(luhot_ctx*, int, const double*, int64_t, double*, double*);
+template int invert_diag_blocks<float, float>(luhot_ctx*, int, const float*, int64_t, float*, float*);
+template int invert_diag_blocks<double, float>(luhot_ctx*, int, const float*, int64_t, double*, double*);
 template int getrs_device<double>(luhot_ctx*, int, int, const double*, int64_t, const int*,
                                   const double*, int64_t, double*, int64_t, int, int);
 template int getrs_device<float>(luhot_ctx*, int, int, const float*, int64_t, const int*,

@@ -238,6 +238,10 @@ struct IrRun {
   double* V;   // (restart + 1) x n
   double* sc;  // device scalars
   double* hsc; // pinned host mirror of sc
+  double* dl64 = nullptr;  // inverses of the diagonal blocks of L and U, FP64 ...
+  double* du64 = nullptr;
+  Tlo* dl = nullptr;       // ... and in the low precision
+  Tlo* du = nullptr;
   int grid_vec;
 
   int launch_check(const char* what) {
@@ -272,10 +276,10 @@ struct IrRun {
     prof_end(ctx, kProfRefine, 0.0, 20.0 * n);
     prof_begin(ctx, kProfTrsv);
     cudaError_t e = launch_trsv_syncfree<double, Tlo>(ctx->stream, lu, ldlo, out, 1, n, 1, true, true, false, false,
-                                                      flags, ticket, ctx->d_status);
+                                                      flags, ticket, ctx->d_status, dl64);
     if (e == cudaSuccess)
       e = launch_trsv_syncfree<double, Tlo>(ctx->stream, lu, ldlo, out, 1, n, 1, false, false, false, false, flags,
-                                            ticket, ctx->d_status);
+                                            ticket, ctx->d_status, du64);
     prof_end(ctx, kProfTrsv, 2.0 * n * (double)n, (double)n * n * sizeof(Tlo) + 32.0 * n);
     if (e != cudaSuccess) return set_error(ctx, LUHOT_ERR_CUDA, std::string("ir sweep: ") + cudaGetErrorString(e));
     return LUHOT_OK;
@@ -292,7 +296,7 @@ struct IrRun {
     prof_end(ctx, kProfRefine, 0.0, (8.0 + sizeof(Tlo)) * n);
     rc = launch_check("ir to-low");
     if (rc) return rc;
-    rc = getrs_apply<Tlo>(ctx, n, 1, lu, ldlo, perm, lo1, 1, lo2, 1, 0, LUHOT_MODE_FAST, low);
+    rc = getrs_apply<Tlo>(ctx, n, 1, lu, ldlo, perm, lo1, 1, lo2, 1, 0, LUHOT_MODE_FAST, low, dl, du);
     if (rc) return rc;
     prof_begin(ctx, kProfRefine);
     if (add_into_out) {
@@ -468,6 +472,18 @@ static int ir_factor(IrRun<float>& s, int precision, luhot_ir_info* info) {
   if (rc) return rc;
   info->singular = sing;
   if (sing >= 0) return set_error(ctx, LUHOT_ERR_SINGULAR, "the low-precision factor is singular");
+  // Inverses of the diagonal blocks for the sweeps of every later solve, in
+  // the factor's precision (plain IR) and widened to FP64 (GMRES-IR).
+  const size_t ne = trsv_inverse_elems(n);
+  rc = ensure_buf(ctx, ctx->dinv_buf, 2 * ne * (sizeof(double) + sizeof(float)));
+  if (rc) return rc;
+  s.dl64 = static_cast<double*>(ctx->dinv_buf.ptr);
+  s.du64 = s.dl64 + ne;
+  s.dl = reinterpret_cast<float*>(s.du64 + ne);
+  s.du = s.dl + ne;
+  rc = invert_diag_blocks<double, float>(ctx, n, s.lu, s.ldlo, s.dl64, s.du64);
+  if (!rc) rc = invert_diag_blocks<float, float>(ctx, n, s.lu, s.ldlo, s.dl, s.du);
+  if (rc) return rc;
   return getrs_perm(ctx, s.piv, n, s.perm);
 }
 

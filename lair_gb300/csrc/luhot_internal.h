@@ -65,6 +65,7 @@ struct luhot_ctx {
   luhot::DevBuf ir_buf[4];                  // refinement: low-precision LU, vectors, indices, rhs
   luhot::DevBuf adj_buf;                    // adjoint: A^T or dA
   luhot::DevBuf tc_buf;                     // tensor-core LU: operand copies + scales
+  luhot::DevBuf dinv_buf;                   // inverses of the 64 x 64 diagonal blocks of L and U
   double* h_scalars = nullptr;              // pinned: scalars read back by the refinement loop
   void* h_piv = nullptr;                    // pinned pivots staging
   size_t h_piv_bytes = 0;
@@ -117,7 +118,14 @@ int getrs_perm(luhot_ctx* ctx, const int* piv, int n, int* perm);
 int trsv_scratch(luhot_ctx* ctx, int n, int** flags, int** ticket);
 template <typename T>
 int getrs_apply(luhot_ctx* ctx, int n, int nrhs, const T* lu, int64_t lda, const int* perm, const T* b,
-                int64_t ldb, T* x, int64_t ldx, int trans, int mode, T* w);
+                int64_t ldb, T* x, int64_t ldx, int trans, int mode, T* w, const T* dinv_l = nullptr,
+                const T* dinv_u = nullptr);
+// Inverses of the diagonal blocks of L (dinv_l) and U (dinv_u) of a
+// row-major LU factor; each holds trsv_inverse_elems(n) elements.  They let
+// the fast untransposed sweeps of getrs_apply replace each 64-step diagonal
+// substitution by a matvec.
+template <typename T, typename TA = T>
+int invert_diag_blocks(luhot_ctx* ctx, int n, const TA* lu, int64_t lda, T* dinv_l, T* dinv_u);
 
 // Held by every C entry point: serialises calls on a context, makes its
 // device current and clears the last error message.

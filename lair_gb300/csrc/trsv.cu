@@ -134,7 +134,8 @@ __device__ __forceinline__ bool wait_ready(const int* flags, int j, DeviceStatus
 template <typename T, typename TA, bool kExact, bool kLower, bool kUnit, bool kTrans, int kNR>
 __global__ void __launch_bounds__(kThreads) trsv_syncfree_kernel(const TA* __restrict__ a, int64_t lda, T* x,
                                                                  int64_t ldx, int n, int nrhs, int* flags,
-                                                                 int* ticket, DeviceStatus* st) {
+                                                                 int* ticket, DeviceStatus* st,
+                                                                 const T* __restrict__ dinv) {
   // Threads per (row, rhs) pair: k split only in fast mode.
   constexpr int kKS = kExact ? 1 : (kNR >= 4 ? 1 : 4 / kNR);
   constexpr int kKLen = kBS / kKS;                      // k columns per thread and tile
@@ -175,6 +176,9 @@ __global__ void __launch_bounds__(kThreads) trsv_syncfree_kernel(const TA* __res
   }
 
   const int nupd = kLower ? I : (nblk - 1 - I);  // blocks before I in sweep order
+  // Inverse of this block's diagonal tile (when given): fetched now, used last.
+  T ireg[kPrefetch];
+  if (!kExact && dinv != nullptr) tile_load<T, T, false>(ireg, dinv + (int64_t)I * kBS * kBS, kBS, 0, 0, kBS, kBS);
   T reg[kPrefetch];
   if (nupd > 0) {
     const int J0 = kLower ? 0 : nblk - 1;
@@ -216,6 +220,44 @@ __global__ void __launch_bounds__(kThreads) trsv_syncfree_kernel(const TA* __res
       }
     }
     __syncthreads();
+  }
+
+  if (!kExact && dinv != nullptr) {
+    // Diagonal block by its precomputed inverse: x(I) = D^-1 xacc, a 64 x 64
+    // matvec split like the updates (no sequential chain on the critical path).
+    __syncthreads();
+    tile_store<T, false>(tile0, ireg);
+#pragma unroll
+    for (int q = 0; q < kPP; ++q) {
+      T v = acc[q];
+      if (kKS > 1) {
+#pragma unroll
+        for (int off = 1; off < kKS; off <<= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+      }
+      if (pon[q] && pk0[q] == 0) xacc[prow[q] * kNR + pc[q]] = v;
+      if (!pon[q] && pk0[q] == 0 && (threadIdx.x + q * kThreads) / kKS < kPairs)
+        xacc[prow[q] * kNR + pc[q]] = T(0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < kPP; ++q) {
+      T v = T(0);
+      for (int kk = 0; kk < kKLen; ++kk) {
+        const int k = pk0[q] + kk;
+        v = fma(tile0[prow[q] * kLds + k], xacc[k * kNR + pc[q]], v);
+      }
+      if (kKS > 1) {
+#pragma unroll
+        for (int off = 1; off < kKS; off <<= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+      }
+      if (pon[q] && pk0[q] == 0) x[(int64_t)(i0 + prow[q]) * ldx + pc[q]] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      st_release_i32(flags + I, 1);
+    }
+    return;
   }
 
   // Sum the k parts of each pair into xacc.
@@ -295,9 +337,13 @@ __global__ void __launch_bounds__(kThreads) trsv_syncfree_kernel(const TA* __res
       if (c < nrhs) x[(int64_t)(i0 + r) * ldx + c] = xout[r * kNR + c];
     }
   }
-  __threadfence();
+  // Every thread's x writes happen before thread 0's fence (CTA barrier); the
+  // gpu-scope fence and release store then publish them together.
   __syncthreads();
-  if (threadIdx.x == 0) st_release_i32(flags + I, 1);
+  if (threadIdx.x == 0) {
+    __threadfence();
+    st_release_i32(flags + I, 1);
+  }
 }
 
 size_t trsv_syncfree_smem(size_t elem) { return (2 * (size_t)kBS * kLds + 2 * (size_t)kBS * kMaxRhs) * elem; }
@@ -305,16 +351,16 @@ int trsv_syncfree_blocks(int n) { return (n + kBS - 1) / kBS; }
 
 template <typename T, typename TA, bool EX, bool LO, bool UN, bool TR>
 static cudaError_t launch_case(cudaStream_t stream, const TA* a, int64_t lda, T* x, int64_t ldx, int n, int nc,
-                               int* flags, int* ticket, DeviceStatus* st) {
+                               int* flags, int* ticket, DeviceStatus* st, const T* dinv) {
   const int nblk = trsv_syncfree_blocks(n);
   const size_t smem = trsv_syncfree_smem(sizeof(T));
   cudaError_t e;
 #define LUHOT_TRSV_NR(NR)                                                                       \
   {                                                                                             \
-    auto k = trsv_syncfree_kernel<T, TA, EX, LO, UN, TR, NR>;                                       \
+    auto k = trsv_syncfree_kernel<T, TA, EX, LO, UN, TR, NR>;                                   \
     e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);        \
     if (e != cudaSuccess) return e;                                                             \
-    k<<<nblk, kThreads, smem, stream>>>(a, lda, x, ldx, n, nc, flags, ticket, st);              \
+    k<<<nblk, kThreads, smem, stream>>>(a, lda, x, ldx, n, nc, flags, ticket, st, dinv);        \
     return cudaGetLastError();                                                                  \
   }
   if (nc == 1) LUHOT_TRSV_NR(1)
@@ -327,9 +373,10 @@ static cudaError_t launch_case(cudaStream_t stream, const TA* a, int64_t lda, T*
 template <typename T, typename TA>
 cudaError_t launch_trsv_syncfree(cudaStream_t stream, const TA* a, int64_t lda, T* x, int64_t ldx, int n, int nrhs,
                                  bool lower, bool unit, bool trans, bool exact, int* flags, int* ticket,
-                                 DeviceStatus* st) {
+                                 DeviceStatus* st, const T* dinv) {
   if (n <= 0 || nrhs <= 0) return cudaSuccess;
   const int nblk = trsv_syncfree_blocks(n);
+  if (exact || trans) dinv = nullptr;  // inverses serve the fast untransposed sweeps only
   for (int c0 = 0; c0 < nrhs; c0 += kMaxRhs) {
     const int nc = std::min(kMaxRhs, nrhs - c0);
     cudaError_t e = cudaMemsetAsync(flags, 0, (size_t)nblk * sizeof(int), stream);
@@ -337,15 +384,15 @@ cudaError_t launch_trsv_syncfree(cudaStream_t stream, const TA* a, int64_t lda, 
     if (e != cudaSuccess) return e;
     T* xc = x + c0;
     if (exact && lower && unit && !trans)
-      e = launch_case<T, TA, true, true, true, false>(stream, a, lda, xc, ldx, n, nc, flags, ticket, st);
+      e = launch_case<T, TA, true, true, true, false>(stream, a, lda, xc, ldx, n, nc, flags, ticket, st, nullptr);
     else if (!exact && lower && unit && !trans)
-      e = launch_case<T, TA, false, true, true, false>(stream, a, lda, xc, ldx, n, nc, flags, ticket, st);
+      e = launch_case<T, TA, false, true, true, false>(stream, a, lda, xc, ldx, n, nc, flags, ticket, st, dinv);
     else if (!exact && !lower && !unit && !trans)
-      e = launch_case<T, TA, false, false, false, false>(stream, a, lda, xc, ldx, n, nc, flags, ticket, st);
+      e = launch_case<T, TA, false, false, false, false>(stream, a, lda, xc, ldx, n, nc, flags, ticket, st, dinv);
     else if (!exact && lower && !unit && trans)
-      e = launch_case<T, TA, false, true, false, true>(stream, a, lda, xc, ldx, n, nc, flags, ticket, st);
+      e = launch_case<T, TA, false, true, false, true>(stream, a, lda, xc, ldx, n, nc, flags, ticket, st, nullptr);
     else if (!exact && !lower && unit && trans)
-      e = launch_case<T, TA, false, false, true, true>(stream, a, lda, xc, ldx, n, nc, flags, ticket, st);
+      e = launch_case<T, TA, false, false, true, true>(stream, a, lda, xc, ldx, n, nc, flags, ticket, st, nullptr);
     else
       return cudaErrorNotSupported;
     if (e != cudaSuccess) return e;
@@ -353,12 +400,70 @@ cudaError_t launch_trsv_syncfree(cudaStream_t stream, const TA* a, int64_t lda, 
   return cudaSuccess;
 }
 
-template cudaError_t launch_trsv_syncfree<double, float>(cudaStream_t, const float*, int64_t, double*, int64_t,
-                                                         int, int, bool, bool, bool, bool, int*, int*,
-                                                         DeviceStatus*);
-template cudaError_t launch_trsv_syncfree<double>(cudaStream_t, const double*, int64_t, double*, int64_t, int, int,
-                                                  bool, bool, bool, bool, int*, int*, DeviceStatus*);
-template cudaError_t launch_trsv_syncfree<float>(cudaStream_t, const float*, int64_t, float*, int64_t, int, int,
-                                                 bool, bool, bool, bool, int*, int*, DeviceStatus*);
+// Inverse of every 64 x 64 diagonal block of a triangular factor (lower unit
+// or upper non-unit), row-major 64 x 64 per block, zero-padded past n.  One
+// CTA per block, one thread per column of the inverse (substitution on the
+// unit vector), all in shared memory.
+template <typename T, typename TA, bool kLower, bool kUnit>
+__global__ void __launch_bounds__(kBS) trsv_invert_diag_kernel(const TA* __restrict__ a, int64_t lda, int n, T* dinv) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* S = reinterpret_cast<T*>(smem_raw);  // [64][65] diagonal block
+  T* Y = S + kBS * kLds;                   // [64][65] inverse, column c owned by thread c
+  const int i0 = blockIdx.x * kBS;
+  const int rows = min(kBS, n - i0);
+  for (int idx = threadIdx.x; idx < kBS * kBS; idx += kBS) {
+    const int r = idx / kBS, c = idx - r * kBS;
+    S[r * kLds + c] = (r < rows && c < rows) ? static_cast<T>(a[(int64_t)(i0 + r) * lda + i0 + c]) : T(0);
+  }
+  __syncthreads();
+  const int c = threadIdx.x;
+  if (kLower) {
+    for (int i = 0; i < kBS; ++i) {
+      T v = T(0);
+      if (c < rows && i < rows && i >= c) {
+        v = (i == c) ? T(1) : T(0);
+        for (int k = c; k < i; ++k) v = fma(-S[i * kLds + k], Y[k * kLds + c], v);
+        if (!kUnit) v = v / S[i * kLds + i];
+      }
+      Y[i * kLds + c] = v;
+    }
+  } else {
+    for (int i = kBS - 1; i >= 0; --i) {
+      T v = T(0);
+      if (c < rows && i < rows && i <= c) {
+        v = (i == c) ? T(1) : T(0);
+        for (int k = i + 1; k <= c; ++k) v = fma(-S[i * kLds + k], Y[k * kLds + c], v);
+        if (!kUnit) v = v / S[i * kLds + i];
+      }
+      Y[i * kLds + c] = v;
+    }
+  }
+  __syncthreads();
+  T* out = dinv + (int64_t)blockIdx.x * kBS * kBS;
+  for (int idx = threadIdx.x; idx < kBS * kBS; idx += kBS) out[idx] = Y[(idx / kBS) * kLds + idx % kBS];
+}
+
+size_t trsv_inverse_elems(int n) { return (size_t)trsv_syncfree_blocks(n) * kBS * kBS; }
+
+template <typename T, typename TA>
+cudaError_t launch_trsv_invert_diag(cudaStream_t stream, const TA* a, int64_t lda, int n, bool lower, T* dinv) {
+  if (n <= 0) return cudaSuccess;
+  const size_t smem = 2 * (size_t)kBS * kLds * sizeof(T);
+  const int nblk = trsv_syncfree_blocks(n);
+  auto k = lower ? trsv_invert_diag_kernel<T, TA, true, true> : trsv_invert_diag_kernel<T, TA, false, false>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k<<<nblk, kBS, smem, stream>>>(a, lda, n, dinv);
+  return cudaGetLastError();
+}
+
+#define LUHOT_TRSV_INST(T, TA)                                                                                  \
+  template cudaError_t launch_trsv_syncfree<T, TA>(cudaStream_t, const TA*, int64_t, T*, int64_t, int, int, bool, \
+                                                   bool, bool, bool, int*, int*, DeviceStatus*, const T*);      \
+  template cudaError_t launch_trsv_invert_diag<T, TA>(cudaStream_t, const TA*, int64_t, int, bool, T*);
+LUHOT_TRSV_INST(double, double)
+LUHOT_TRSV_INST(float, float)
+LUHOT_TRSV_INST(double, float)
+#undef LUHOT_TRSV_INST
 
 }  // namespace luhot

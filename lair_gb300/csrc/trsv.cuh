@@ -15,10 +15,20 @@ int trsv_syncfree_blocks(int n);
 // op(A) x = b in place for nrhs columns of x (row-major, ldx); flags must hold
 // trsv_syncfree_blocks(n) ints and ticket one int of device scratch (both
 // cleared by this call); st supplies the wait limit and records a timeout.
-// TA is the storage type of the factor (it may be narrower than T).
+// TA is the storage type of the factor (it may be narrower than T).  dinv,
+// when not null, holds the inverses of the 64 x 64 diagonal blocks of this
+// triangle (launch_trsv_invert_diag) and replaces the sequential diagonal
+// solve by a matvec; it is ignored in exact mode and for transposed sweeps.
 template <typename T, typename TA = T>
 cudaError_t launch_trsv_syncfree(cudaStream_t stream, const TA* a, int64_t lda, T* x, int64_t ldx, int n, int nrhs,
                                  bool lower, bool unit, bool trans, bool exact, int* flags, int* ticket,
-                                 DeviceStatus* st);
+                                 DeviceStatus* st, const T* dinv = nullptr);
+
+// Elements of the diagonal-block inverses for order n.
+size_t trsv_inverse_elems(int n);
+// Inverses of the diagonal blocks of the unit lower (lower) or non-unit upper
+// triangle of a row-major LU factor.
+template <typename T, typename TA = T>
+cudaError_t launch_trsv_invert_diag(cudaStream_t stream, const TA* a, int64_t lda, int n, bool lower, T* dinv);
 
 }  // namespace luhot
