@@ -233,6 +233,40 @@ int luhot_dgetrs_dev(luhot_ctx* ctx, int64_t n, int64_t nrhs, const double* d_lu
 int luhot_sgetrs_dev(luhot_ctx* ctx, int64_t n, int64_t nrhs, const float* d_lu, int64_t lda,
                      const int32_t* d_piv, float* d_b, int64_t ldb, int trans, int mode);
 
+/* ---- Device-resident factors ------------------------------------------
+ * Replaces lair's lu::Factorized (src/decomposition/lu.rs:12-20, 156-171) and
+ * Factorized::solve (lu.rs:87-98) for callers that solve repeatedly: the
+ * factored array stays on the GPU with its pivots, the row permutation
+ * composed from them and (fast mode) the inverses of the 64 x 64 diagonal
+ * blocks, so each solve moves only b and x.  The pivots and the singular step
+ * (-1 = None) are returned at creation, as Factorized::from fills its fields;
+ * the factored array reaches the host only through luhot_factor_read (what
+ * lair's p()/l()/u(), lu.rs:28-72, read).  A factor belongs to the context
+ * that made it: destroy it before the context; its calls serialise on the
+ * context's lock and run on the context's stream.  Solves need m <= n (lair's
+ * getrs asserts a.nrows() == p.len(), src/lapack/getrs.rs:18). */
+typedef struct luhot_factor luhot_factor;
+int luhot_dfactor_create(luhot_ctx* ctx, int64_t m, int64_t n, const double* a, int64_t rs, int64_t cs, int mode,
+                         uint64_t* piv, int64_t* singular, luhot_factor** out);
+int luhot_sfactor_create(luhot_ctx* ctx, int64_t m, int64_t n, const float* a, int64_t rs, int64_t cs, int mode,
+                         uint64_t* piv, int64_t* singular, luhot_factor** out);
+/* Same from a row-major device matrix (not modified). */
+int luhot_dfactor_create_dev(luhot_ctx* ctx, int64_t m, int64_t n, const double* d_a, int64_t lda, int mode,
+                             uint64_t* piv, int64_t* singular, luhot_factor** out);
+/* X = A^-1 B (trans: A^-T B), host B and X with element strides (they may
+ * be the same array). */
+int luhot_dfactor_solve(luhot_factor* f, int64_t nrhs, const double* b, int64_t b_rs, int64_t b_cs, double* x,
+                        int64_t x_rs, int64_t x_cs, int trans);
+int luhot_sfactor_solve(luhot_factor* f, int64_t nrhs, const float* b, int64_t b_rs, int64_t b_cs, float* x,
+                        int64_t x_rs, int64_t x_cs, int trans);
+/* Device B (m x nrhs row-major, ldb), overwritten by X. */
+int luhot_dfactor_solve_dev(luhot_factor* f, int64_t nrhs, double* d_b, int64_t ldb, int trans);
+/* Copy the factored array (L\U, m x n) to a host array with element strides. */
+int luhot_factor_read(luhot_factor* f, void* a, int64_t rs, int64_t cs);
+/* The factor's device storage (row-major, lda) and int32 pivots. */
+int luhot_factor_device(const luhot_factor* f, const void** d_lu, int64_t* lda, const int32_t** d_piv);
+void luhot_factor_destroy(luhot_factor* f);
+
 /* Scratch held by luhot_dgetrs_dev_noalloc in a static device array. */
 #define LUHOT_NOALLOC_SCRATCH_BYTES (4u << 20)
 

@@ -71,6 +71,18 @@ SIGNATURES = {
     "luhot_batch_tuning": (_i32, [_vp, _vp, _vp]),
     "luhot_batch_solve": (_i32, [_vp, _vp, _vp, _vp, _vp]),
     "luhot_batch_solve_host": (_i32, [_vp, _vp, _vp, _vp, _vp]),
+    "luhot_dfactor_create": (_i32, [_vp, _i64, _i64, _vp, _i64, _i64, _i32, _vp, ctypes.POINTER(_i64),
+                                    ctypes.POINTER(_vp)]),
+    "luhot_sfactor_create": (_i32, [_vp, _i64, _i64, _vp, _i64, _i64, _i32, _vp, ctypes.POINTER(_i64),
+                                    ctypes.POINTER(_vp)]),
+    "luhot_dfactor_create_dev": (_i32, [_vp, _i64, _i64, _vp, _i64, _i32, _vp, ctypes.POINTER(_i64),
+                                        ctypes.POINTER(_vp)]),
+    "luhot_dfactor_solve": (_i32, [_vp, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _i32]),
+    "luhot_sfactor_solve": (_i32, [_vp, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _i32]),
+    "luhot_dfactor_solve_dev": (_i32, [_vp, _i64, _vp, _i64, _i32]),
+    "luhot_factor_read": (_i32, [_vp, _vp, _i64, _i64]),
+    "luhot_factor_device": (_i32, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_i64), ctypes.POINTER(_vp)]),
+    "luhot_factor_destroy": (None, [_vp]),
     "luhot_dgetrs_dev_noalloc": (_i32, [_i64, _i64, _vp, _i64, _vp, _vp, _i64, _i32, _i32, _vp]),
 }
 
