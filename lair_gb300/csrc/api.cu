@@ -375,10 +375,7 @@ int luhot_create(luhot_ctx** out, int device) {
   ok = ok && cudaMalloc(&ctx->d_status, sizeof(DeviceStatus)) == cudaSuccess;
   ok = ok && cudaMallocHost(&ctx->h_status, sizeof(DeviceStatus)) == cudaSuccess;
   ok = ok && cudaMallocHost(&ctx->h_scalars, 256 * sizeof(double)) == cudaSuccess;
-  const size_t scratch = (2 * (size_t)kMaxPanelCtas + 2 * (size_t)kMaxPanelCtas * kMaxPanelWidth +
-                          2 * (size_t)kMaxPanelWidth) * sizeof(double) +
-                         2 * (size_t)kMaxPanelCtas * sizeof(int);
-  ok = ok && cudaMalloc(&ctx->panel_scratch, scratch) == cudaSuccess;
+  ok = ok && cudaMalloc(&ctx->panel_scratch, kPanelScratchBytes) == cudaSuccess;
   if (!ok || ctx->num_sms > kMaxPanelCtas) {
     cudaGetLastError();
     luhot_destroy(ctx);

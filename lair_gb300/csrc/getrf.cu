@@ -7,9 +7,11 @@
 //
 // One block step k0 (panel width w) runs four kernels:
 //   1. panel_kernel   cooperative; factors rows [k0, m) x cols [k0, k0+w) held
-//                     in shared memory across all CTAs; one bounded grid
-//                     barrier per column for the pivot search (warp-shuffle
-//                     iamax, then a deterministic reduce over CTAs).
+//                     in shared memory across all CTAs; per column one
+//                     exchange of step-tagged candidates through L2 (integer
+//                     pivot keys, warp-shuffle reduce, deterministic order),
+//                     row interchanges as id swaps, and the update of the
+//                     previous step overlapping the exchange.
 //   2. laswp_kernel   applies the w interchanges to the columns left and
 //                     right of the panel (coalesced 16-byte row moves).
 //   3. trsm_kernel    U12 <- L11^-1 A12 (unit lower).
@@ -61,180 +63,449 @@ struct PanelArgs {
   int rows_per;   // panel rows owned by each CTA
   int lds;        // shared-memory row stride (elements)
   int* piv;       // device pivots (global row index per step)
-  T* cand_val;    // [2][P]
-  int* cand_idx;  // [2][P]
-  T* cand_row;    // [2][P][w]   row segment of each CTA's candidate
-  T* row_ul;      // [2][w]      segment of row ul before the swap
+  unsigned long long* slots;  // [2][kMaxPanelCtas][kPanelSlotWords] exchange words
   DeviceStatus* st;
-  unsigned int bar_base;
 };
 
-// First index of the largest |x| with lair's strict `>` (src/blas/iamax.rs:6-21):
-// larger value wins, equal values keep the smaller row.  NaN never compares
-// greater, so it never wins.  (0, INT_MAX) means "no positive entry".
+// Pivot search keys.  lair's iamax (src/blas/iamax.rs:6-21) takes the first
+// index of the largest |x| with a strict `>`: larger value wins, equal values
+// keep the smaller row, NaN never wins, and an all-zero/NaN column means a
+// singular step.  For |x| >= 0 the IEEE bit pattern orders like the value,
+// so the search compares integers (on the integer pipe; FP64 compares are
+// slow on this part): key = bits of |x|, or 0 for NaN.  (key, row) ordered by
+// key descending then row ascending is a total order, so any reduction tree
+// gives the same answer; key 0 means "no positive entry".
 template <typename T>
-__device__ __forceinline__ void iamax_combine(T& v, int& i, T v2, int i2) {
-  if (v2 > v || (v2 == v && i2 < i)) {
-    v = v2;
+struct PivotKey;
+template <>
+struct PivotKey<float> {
+  using K = unsigned int;
+  __device__ static K of(float x) {
+    const unsigned int b = __float_as_uint(x) & 0x7fffffffu;
+    return b > 0x7f800000u ? 0u : b;
+  }
+  __device__ static K shfl_xor(K k, int off) { return __shfl_xor_sync(0xffffffffu, k, off); }
+  __device__ static K shfl(K k, int src) { return __shfl_sync(0xffffffffu, k, src); }
+};
+template <>
+struct PivotKey<double> {
+  using K = unsigned long long;
+  __device__ static K of(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
+    return b > 0x7ff0000000000000ull ? 0ull : b;
+  }
+  __device__ static K shfl_xor(K k, int off) { return __shfl_xor_sync(0xffffffffu, k, off); }
+  __device__ static K shfl(K k, int src) { return __shfl_sync(0xffffffffu, k, src); }
+};
+
+template <typename K>
+__device__ __forceinline__ void key_combine(K& k, int& i, int& s, K k2, int i2, int s2) {
+  if (k2 > k || (k2 == k && i2 < i)) {
+    k = k2;
     i = i2;
+    s = s2;
+  }
+}
+template <typename T>
+__device__ __forceinline__ void key_reduce_warp(typename PivotKey<T>::K& k, int& i, int& s, int width) {
+  for (int off = width >> 1; off > 0; off >>= 1)
+    key_combine(k, i, s, PivotKey<T>::shfl_xor(k, off), __shfl_xor_sync(0xffffffffu, i, off),
+                __shfl_xor_sync(0xffffffffu, s, off));
+}
+
+// Exchange words: payload in the low 32 bits, the step tag in the high 32.
+// A reader accepts a word only when its tag is the step it waits for, so no
+// fence or counter orders the writers and readers: each 8-byte word is
+// written and read whole.  Tags are step + 1 and the slots are zeroed before
+// each factorization, so a stale word never carries a live tag.
+__device__ __forceinline__ unsigned long long ld_word(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_word(unsigned long long* p, unsigned int bits, unsigned int tag) {
+  const unsigned long long v = ((unsigned long long)tag << 32) | bits;
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ bool word_ok(unsigned long long v, unsigned int tag) {
+  return (unsigned int)(v >> 32) == tag;
+}
+// Values and keys as one (FP32) or two (FP64) tagged words.
+template <typename T>
+struct Tagged;
+template <>
+struct Tagged<float> {
+  static constexpr int kWords = 1;
+  __device__ static void put(unsigned long long* p, float v, unsigned int tag) { st_word(p, __float_as_uint(v), tag); }
+  __device__ static bool get(const unsigned long long* p, unsigned int tag, float& v) {
+    const unsigned long long x = ld_word(p);
+    v = __uint_as_float((unsigned int)x);
+    return word_ok(x, tag);
+  }
+  __device__ static void put_key(unsigned long long* p, unsigned int k, unsigned int tag) { st_word(p, k, tag); }
+  __device__ static bool get_key(const unsigned long long* p, unsigned int tag, unsigned int& k) {
+    const unsigned long long x = ld_word(p);
+    k = (unsigned int)x;
+    return word_ok(x, tag);
+  }
+};
+template <>
+struct Tagged<double> {
+  static constexpr int kWords = 2;
+  __device__ static void put(unsigned long long* p, double v, unsigned int tag) {
+    put_key(p, (unsigned long long)__double_as_longlong(v), tag);
+  }
+  __device__ static bool get(const unsigned long long* p, unsigned int tag, double& v) {
+    unsigned long long b;
+    const bool ok = get_key(p, tag, b);
+    v = __longlong_as_double((long long)b);
+    return ok;
+  }
+  __device__ static void put_key(unsigned long long* p, unsigned long long k, unsigned int tag) {
+    st_word(p, (unsigned int)(k >> 32), tag);
+    st_word(p + 1, (unsigned int)k, tag);
+  }
+  __device__ static bool get_key(const unsigned long long* p, unsigned int tag, unsigned long long& k) {
+    const unsigned long long hi = ld_word(p), lo = ld_word(p + 1);
+    k = ((unsigned long long)(unsigned int)hi << 32) | (unsigned int)lo;
+    return word_ok(hi, tag) && word_ok(lo, tag);
+  }
+};
+
+// Give up a wait: record the step, raise abort so every other wait of the
+// launch returns at once.  Called by one lane.
+__device__ __forceinline__ void panel_give_up(DeviceStatus* st, int step) {
+  atomicCAS(&st->error, kDevOk, kDevBarrierTimeout);
+  atomicExch(&st->timeout_where, (unsigned long long)step);
+  atomicExch(&st->abort, 1);
+}
+// Warp-uniform test of the wait limit and of another CTA's abort.
+__device__ __forceinline__ bool panel_wait_over(DeviceStatus* st, unsigned long long t0) {
+  const int late = (global_timer_ns() - t0 > st->timeout_ns) ? 1 : 0;
+  return __shfl_sync(0xffffffffu, late, 0) != 0 || __any_sync(0xffffffffu, ld_relaxed_i32(&st->abort) != 0);
+}
+
+// A[r][c] -= A[r][jj] * u[c] for the rows [r0, nloc) other than `skip` and
+// the columns [c0, w), by threads t of nt (a multiple of 32).  FP64 flattens
+// (row, column) pairs so every lane is busy (the FP64 pipe bounds it); FP32
+// gives each warp whole rows, lanes along the columns (no index arithmetic
+// per element; latency bounds it).
+template <typename T, bool kExact>
+__device__ __forceinline__ void panel_update(T* S, int lds, int r0, int nloc, int skip, int jj, int c0, int w,
+                                             const T* u, int t, int nt) {
+  const int wc = w - c0;
+  if (wc <= 0 || r0 >= nloc) return;
+  if constexpr (sizeof(T) == 8) {
+    const int total = (nloc - r0) * wc;
+    const int step_r = nt / wc, step_c = nt - step_r * wc;
+    int r = r0 + t / wc, c = t - (t / wc) * wc;
+    for (int idx = t; idx < total; idx += 2 * nt) {
+      const int ra = r, ca = c;
+      r += step_r;
+      c += step_c;
+      if (c >= wc) {
+        c -= wc;
+        ++r;
+      }
+      const int rb = r, cb = c;
+      const bool on_b = idx + nt < total;
+      r += step_r;
+      c += step_c;
+      if (c >= wc) {
+        c -= wc;
+        ++r;
+      }
+      T xa = T(0), la = T(0), ua = T(0), xb = T(0), lb = T(0), ub = T(0);
+      const bool do_a = ra != skip, do_b = on_b && rb != skip;
+      if (do_a) {
+        xa = S[ra * lds + c0 + ca];
+        la = S[ra * lds + jj];
+        ua = u[c0 + ca];
+      }
+      if (do_b) {
+        xb = S[rb * lds + c0 + cb];
+        lb = S[rb * lds + jj];
+        ub = u[c0 + cb];
+      }
+      if (do_a) S[ra * lds + c0 + ca] = upd<kExact>(xa, la, ua);
+      if (do_b) S[rb * lds + c0 + cb] = upd<kExact>(xb, lb, ub);
+    }
+  } else {
+    const int lane = t & 31, wi = t >> 5, nw = nt >> 5;
+    T ur[kMaxPanelWidth / 32];
+#pragma unroll
+    for (int q = 0; q < kMaxPanelWidth / 32; ++q) {
+      const int c = c0 + lane + 32 * q;
+      ur[q] = c < w ? u[c] : T(0);
+    }
+    for (int r = r0 + wi; r < nloc; r += 2 * nw) {
+      const int rb = r + nw;
+      const bool a_on = r != skip, b_on = rb < nloc && rb != skip;
+      T* ra = S + r * lds;
+      T* rbp = S + (b_on ? rb : r) * lds;
+      const T la = ra[jj], lb = rbp[jj];
+#pragma unroll
+      for (int q = 0; q < kMaxPanelWidth / 32; ++q) {
+        const int c = c0 + lane + 32 * q;
+        if (32 * q < wc && c < w) {
+          const T xa = ra[c], xb = rbp[c];
+          if (a_on) ra[c] = upd<kExact>(xa, la, ur[q]);
+          if (b_on) rbp[c] = upd<kExact>(xb, lb, ur[q]);
+        }
+      }
+    }
   }
 }
 
+// Cooperative panel factorization: rows [k0, m) x columns [k0, k0 + w) are
+// spread over P CTAs (rows_per each) and held in shared memory for the whole
+// panel.  Rows are never moved between CTAs during the panel: each CTA keeps
+// the global row index (id) of every row it holds, and an interchange of rows
+// ul and pr only swaps two ids.  The row that receives id ul is the pivot
+// row; its CTA moves it into its block of retired rows [0, r0) (a local move).
+// At the end every row is written to the global row its id names.
+//
+// Per column j (elimination step ul = k0 + j), with the update of step j-1
+// to columns j+1.. still pending for all rows but this CTA's candidate row:
+//   warp 0:     finish the candidate row's pending update; publish its key
+//               (|pivot| bits), row id, segment j.. and 1/pivot as tagged
+//               words; poll the P headers until all carry this step's tag,
+//               folding them into the winner; read the winner's segment and
+//               reciprocal; relabel the ids of rows ul and pr.
+//   warps 1-7:  meanwhile, the pending update of step j-1 (columns j+1..),
+//               which thus overlaps the exchange.
+//   barrier;    the pivot row's CTA retires it; all warps scale column j,
+//               update column j+1 only and find its candidates; barrier.
+// The arithmetic and its order per element are those of lair's
+// getrf_row_major (src/lapack/getrf.rs:56-89): 1/p rounded, l = a*(1/p)
+// rounded, a - l*u (separately rounded in exact mode), steps in order.
 template <typename T, bool kExact>
 __global__ void __launch_bounds__(256) panel_kernel(PanelArgs<T> p) {
+  using K = typename PivotKey<T>::K;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* S = reinterpret_cast<T*>(smem_raw);              // [rows_per][lds]
-  T* seg = S + (size_t)p.rows_per * p.lds;            // [w] pivot row segment
-  __shared__ T red_v[32];
-  __shared__ int red_i[32];
-  __shared__ int s_piv;
-  __shared__ T s_max;
-  __shared__ int s_win;
+  T* S = reinterpret_cast<T*>(smem_raw);                        // [rows_per][lds]
+  T* segb = S + (size_t)p.rows_per * p.lds;                     // [2][kMaxPanelWidth] pivot rows
+  int* ids = reinterpret_cast<int*>(segb + 2 * kMaxPanelWidth);  // [rows_per] global row of each slot
+  __shared__ K red_k[8];
+  __shared__ int red_i[8], red_s[8];
+  __shared__ int s_ok, s_r0, s_pivoted, s_ret;
+  __shared__ T s_recip;
 
+  constexpr unsigned kFull = 0xffffffffu;
+  constexpr int kWarps = 8;
+  constexpr int kW = Tagged<T>::kWords;
+  constexpr int kHdr = kPanelHeaderWords;
   const int P = gridDim.x;
   const int b = blockIdx.x;
   const int tid = threadIdx.x;
-  const int nthr = blockDim.x;
-  const int lane = tid & 31, warp = tid >> 5, nwarps = nthr >> 5;
+  const int lane = tid & 31, warp = tid >> 5;
   const int r_begin = p.k0 + b * p.rows_per;
-  const int r_end = min(p.m, r_begin + p.rows_per);
-  const int nloc = max(0, r_end - r_begin);
+  const int nloc = max(0, min(p.m, r_begin + p.rows_per) - r_begin);
   const int w = p.w;
+  const int lds = p.lds;
 
-  // Stage this CTA's rows of the panel in shared memory.
-  for (int idx = tid; idx < nloc * w; idx += nthr) {
+  for (int idx = tid; idx < nloc * w; idx += blockDim.x) {
     const int r = idx / w, c = idx - r * w;
-    S[r * p.lds + c] = p.a[(int64_t)(r_begin + r) * p.lda + p.k0 + c];
+    S[r * lds + c] = p.a[(int64_t)(r_begin + r) * p.lda + p.k0 + c];
+  }
+  for (int r = tid; r < nloc; r += blockDim.x) ids[r] = r_begin + r;
+  if (tid == 0) s_r0 = 0;
+  __syncthreads();
+  {
+    // Column 0 candidates.
+    K bk = 0;
+    int bi = INT_MAX, bs = -1;
+    for (int r = tid; r < nloc; r += blockDim.x) key_combine(bk, bi, bs, PivotKey<T>::of(S[r * lds]), ids[r], r);
+    key_reduce_warp<T>(bk, bi, bs, 32);
+    if (lane == 0) {
+      red_k[warp] = bk;
+      red_i[warp] = bi;
+      red_s[warp] = bs;
+    }
   }
   __syncthreads();
 
-  unsigned int target = p.bar_base;
+  const int nq = (P + 31) / 32;  // candidate CTAs per lane in the poll
+  int dj = -1;                   // step whose update of columns dj+2.. is pending
+  int dr0 = 0;                   // first active row of that step
   for (int j = 0; j < w; ++j) {
     const int ul = p.k0 + j;
-    const int par = j & 1;
-    // Local pivot search over owned rows >= ul in column j.
-    T bv = T(0);
-    int bi = INT_MAX;
-    for (int r = max(0, ul - r_begin) + tid; r < nloc; r += nthr) {
-      const T v = fabs(S[r * p.lds + j]);
-      if (v > bv) {  // rows visited in increasing order per thread
-        bv = v;
-        bi = r_begin + r;
-      }
-    }
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-      const T v2 = __shfl_down_sync(0xffffffffu, bv, off);
-      const int i2 = __shfl_down_sync(0xffffffffu, bi, off);
-      iamax_combine(bv, bi, v2, i2);
-    }
-    if (lane == 0) {
-      red_v[warp] = bv;
-      red_i[warp] = bi;
-    }
-    __syncthreads();
-    if (tid == 0) {
-      for (int q = 1; q < nwarps; ++q) iamax_combine(bv, bi, red_v[q], red_i[q]);
-      s_max = bv;
-      s_win = bi;
-    }
-    __syncthreads();
-    // Publish the candidate, its row segment, and (owner only) row ul.
-    const int cbi = s_win;
-    if (tid == 0) {
-      p.cand_val[par * P + b] = s_max;
-      p.cand_idx[par * P + b] = cbi;
-    }
-    if (cbi != INT_MAX) {
-      const int r = cbi - r_begin;
-      for (int c = tid; c < w; c += nthr) p.cand_row[((size_t)par * P + b) * w + c] = S[r * p.lds + c];
-    }
-    if (ul >= r_begin && ul < r_end) {
-      const int r = ul - r_begin;
-      for (int c = tid; c < w; c += nthr) p.row_ul[(size_t)par * w + c] = S[r * p.lds + c];
-    }
-    target += P;
-    if (!grid_barrier(p.st, target, (unsigned long long)ul)) return;
-
-    // Every CTA reduces the P candidates in the same order: same answer.
+    const unsigned int tag = (unsigned int)ul + 1u;
+    unsigned long long* slots = p.slots + (size_t)(j & 1) * kMaxPanelCtas * kPanelSlotWords;
+    T* seg = segb + (j & 1) * kMaxPanelWidth;
+    // The CTA's candidate for column j (every warp reduces the same eight).
+    K ck = lane < kWarps ? red_k[lane] : K(0);
+    int ci = lane < kWarps ? red_i[lane] : INT_MAX;
+    int cs = lane < kWarps ? red_s[lane] : -1;
+    key_reduce_warp<T>(ck, ci, cs, kWarps);
+    ck = PivotKey<T>::shfl(ck, 0);
+    ci = __shfl_sync(kFull, ci, 0);
+    cs = __shfl_sync(kFull, cs, 0);
     if (warp == 0) {
-      T v = T(0);
+      if (dj >= 0 && cs >= 0) {
+        // The candidate row's pending update, before it is published.
+        const T* up = segb + (dj & 1) * kMaxPanelWidth;
+        const T l = S[cs * lds + dj];
+        for (int c = dj + 2 + lane; c < w; c += 32) S[cs * lds + c] = upd<kExact>(S[cs * lds + c], l, up[c]);
+        __syncwarp();
+      }
+      // Publish: segment j.., the header, then 1/pivot (its division
+      // overlaps the other CTAs' publishing).
+      unsigned long long* mine = slots + (size_t)b * kPanelSlotWords;
+      if (cs >= 0)
+        for (int c = j + lane; c < w; c += 32) Tagged<T>::put(mine + kHdr + c * kW, S[cs * lds + c], tag);
+      if (lane == 0) {
+        Tagged<T>::put_key(mine, ck, tag);
+        st_word(mine + 2, (unsigned int)ci, tag);
+        if (ck > 0) Tagged<T>::put(mine + 3, T(1) / S[cs * lds + j], tag);
+      }
+      // Poll every CTA's header; fold each one in as soon as it is current.
+      K k = 0;
       int i = INT_MAX, win = -1;
-      for (int q = lane; q < P; q += 32) {
-        const T v2 = ld_cg(&p.cand_val[par * P + q]);
-        const int i2 = ld_cg(&p.cand_idx[par * P + q]);
-        if (v2 > v || (v2 == v && i2 < i)) {
-          v = v2;
-          i = i2;
-          win = q;
+      unsigned pending = 0;
+      for (int q = 0; q < nq; ++q)
+        if (lane + 32 * q < P) pending |= 1u << q;
+      const unsigned long long t0 = global_timer_ns();
+      unsigned int spins = 0;
+      int ok = 1;
+      while (true) {
+        for (int q = 0; q < nq; ++q) {
+          if (!(pending & (1u << q))) continue;
+          const int cta = lane + 32 * q;
+          const unsigned long long* h = slots + (size_t)cta * kPanelSlotWords;
+          K hk;
+          const bool kok = Tagged<T>::get_key(h, tag, hk);
+          const unsigned long long hi = ld_word(h + 2);
+          if (kok && word_ok(hi, tag)) {
+            key_combine(k, i, win, hk, (int)(unsigned int)hi, cta);
+            pending &= ~(1u << q);
+          }
+        }
+        if (__all_sync(kFull, pending == 0)) break;
+        if ((++spins & 15u) == 0 && panel_wait_over(p.st, t0)) {
+          if (lane == 0 && !ld_relaxed_i32(&p.st->abort)) panel_give_up(p.st, ul);
+          ok = 0;
+          break;
         }
       }
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) {
-        const T v2 = __shfl_down_sync(0xffffffffu, v, off);
-        const int i2 = __shfl_down_sync(0xffffffffu, i, off);
-        const int w2 = __shfl_down_sync(0xffffffffu, win, off);
-        if (v2 > v || (v2 == v && i2 < i)) {
-          v = v2;
-          i = i2;
-          win = w2;
+      int ret = -1;
+      if (ok) {
+        key_reduce_warp<T>(k, i, win, 32);
+        const int pr = (k > 0) ? i : ul;
+        if (k > 0) {
+          // The pivot row's columns j.. and 1/pivot from the winner's slot.
+          const unsigned long long* ws = slots + (size_t)win * kPanelSlotWords;
+          while (true) {
+            bool got = true;
+            for (int c = j + lane; c < w; c += 32) {
+              T x;
+              got = Tagged<T>::get(ws + kHdr + c * kW, tag, x) && got;
+              seg[c] = x;
+            }
+            if (lane == 0) {
+              T rc;
+              got = Tagged<T>::get(ws + 3, tag, rc) && got;
+              s_recip = rc;
+            }
+            if (__all_sync(kFull, got)) break;
+            if (panel_wait_over(p.st, t0)) {
+              if (lane == 0 && !ld_relaxed_i32(&p.st->abort)) panel_give_up(p.st, ul);
+              ok = 0;
+              break;
+            }
+          }
+        } else if (b == 0 && lane == 0) {
+          // lair: max == 0 -> the step is singular, no swap, no update
+          // (src/lapack/getrf.rs:72-73).  The last such step wins.
+          atomicMax(&p.st->singular, ul);
+        }
+        if (ok) {
+          // Relabel: the row with id ul takes id pr and the row with id pr
+          // takes id ul; the latter (the pivot row) retires after the barrier.
+          int found = 0;
+          for (int r = s_r0 + lane; r < nloc; r += 32) {
+            const int id = ids[r];
+            if (id == ul) found |= (r + 1) << 16;
+            if (id == pr) found |= r + 1;
+          }
+          found = __reduce_or_sync(kFull, found);
+          const int s_ul = (found >> 16) - 1, s_pr = (found & 0xffff) - 1;
+          ret = s_ul;
+          if (pr != ul) {
+            if (lane == 0) {
+              if (s_ul >= 0) ids[s_ul] = pr;
+              if (s_pr >= 0) ids[s_pr] = ul;
+            }
+            ret = s_pr;
+          }
+          if (b == 0 && lane == 0) p.piv[ul] = pr;
+          if (lane == 0) s_pivoted = k > 0 ? 1 : 0;
         }
       }
       if (lane == 0) {
-        s_max = v;
-        s_piv = (v > T(0)) ? i : ul;
-        s_win = win;
+        s_ok = ok;
+        s_ret = ret;
       }
+    } else if (dj >= 0) {
+      panel_update<T, kExact>(S, lds, dr0, nloc, cs, dj, dj + 2, w, segb + (dj & 1) * kMaxPanelWidth, tid - 32,
+                              blockDim.x - 32);
     }
     __syncthreads();
-    const T maxv = s_max;
-    const int pr = s_piv;
-    if (!(maxv > T(0))) {
-      // lair: max == 0 -> record the step as singular, no swap, no update
-      // (src/lapack/getrf.rs:72-73).  The last such step wins.
-      if (b == 0 && tid == 0) {
-        p.piv[ul] = ul;
-        atomicMax(&p.st->singular, ul);
+    if (!s_ok) return;
+    // Retire the pivot row into slot r0.
+    int r0 = s_r0;
+    const int ret = s_ret;
+    if (ret >= 0) {
+      if (warp == 0 && ret != r0) {
+        for (int c = lane; c < w; c += 32) {
+          const T x = S[ret * lds + c];
+          S[ret * lds + c] = S[r0 * lds + c];
+          S[r0 * lds + c] = x;
+        }
+        if (lane == 0) {
+          const int t = ids[ret];
+          ids[ret] = ids[r0];
+          ids[r0] = t;
+        }
       }
-      continue;
+      ++r0;
+      __syncthreads();
+      if (tid == 0) s_r0 = r0;
     }
-    const int win = s_win;
-    for (int c = tid; c < w; c += nthr) seg[c] = ld_cg(&p.cand_row[((size_t)par * P + win) * w + c]);
-    __syncthreads();
-    if (pr != ul) {
-      if (ul >= r_begin && ul < r_end) {
-        const int r = ul - r_begin;
-        for (int c = tid; c < w; c += nthr) S[r * p.lds + c] = seg[c];
+
+    // Scale column j, update column j+1 only, find its candidates.
+    K bk = 0;
+    int bi = INT_MAX, bs = -1;
+    if (s_pivoted) {
+      const T recip = s_recip;
+      for (int r = r0 + tid; r < nloc; r += blockDim.x) S[r * lds + j] = mul_rn(S[r * lds + j], recip);
+      if (j + 1 < w) {
+        const T u1 = seg[j + 1];
+        for (int r = r0 + tid; r < nloc; r += blockDim.x) {
+          const T v = upd<kExact>(S[r * lds + j + 1], S[r * lds + j], u1);
+          S[r * lds + j + 1] = v;
+          key_combine(bk, bi, bs, PivotKey<T>::of(v), ids[r], r);
+        }
       }
-      if (pr >= r_begin && pr < r_end) {
-        const int r = pr - r_begin;
-        for (int c = tid; c < w; c += nthr) S[r * p.lds + c] = ld_cg(&p.row_ul[(size_t)par * w + c]);
-      }
+      dj = j;
+      dr0 = r0;
+    } else {
+      if (j + 1 < w)
+        for (int r = r0 + tid; r < nloc; r += blockDim.x)
+          key_combine(bk, bi, bs, PivotKey<T>::of(S[r * lds + j + 1]), ids[r], r);
+      dj = -1;
     }
-    if (b == 0 && tid == 0) p.piv[ul] = pr;
-    __syncthreads();
-    // Scale the column below the pivot by the reciprocal (1/pivot rounded,
-    // then a rounded multiply: src/lapack/getrf.rs:76-81).
-    const T recip = T(1) / seg[j];
-    const int r0 = max(0, ul + 1 - r_begin);
-    for (int r = r0 + tid; r < nloc; r += nthr) S[r * p.lds + j] = mul_rn(S[r * p.lds + j], recip);
-    __syncthreads();
-    // Rank-1 update of the panel columns right of j.
-    const int wr = w - j - 1;
-    if (wr > 0) {
-      const int total = (nloc - r0) * wr;
-      for (int idx = tid; idx < total; idx += nthr) {
-        const int r = r0 + idx / wr;
-        const int c = j + 1 + idx % wr;
-        S[r * p.lds + c] = upd<kExact>(S[r * p.lds + c], S[r * p.lds + j], seg[c]);
-      }
+    key_reduce_warp<T>(bk, bi, bs, 32);
+    if (lane == 0) {
+      red_k[warp] = bk;
+      red_i[warp] = bi;
+      red_s[warp] = bs;
     }
     __syncthreads();
   }
-  __syncthreads();
-  for (int idx = tid; idx < nloc * w; idx += nthr) {
+  for (int idx = tid; idx < nloc * w; idx += blockDim.x) {
     const int r = idx / w, c = idx - r * w;
-    p.a[(int64_t)(r_begin + r) * p.lda + p.k0 + c] = S[r * p.lds + c];
+    p.a[(int64_t)ids[r] * p.lda + p.k0 + c] = S[r * lds + c];
   }
 }
 
@@ -445,12 +716,12 @@ __global__ void __launch_bounds__(256) gemm_dmma_kernel(double* a, int64_t lda, 
 // ---------------------------------------------------------------------------
 template <typename T>
 static size_t panel_smem_bytes(int rows_per, int w) {
-  return ((size_t)rows_per * (w + 1) + w) * sizeof(T);
+  return ((size_t)rows_per * (w + 1) + 2 * kMaxPanelWidth) * sizeof(T) + (size_t)rows_per * sizeof(int);
 }
 
 template <typename T, bool kExact>
 static int launch_panel(luhot_ctx* ctx, T* a, int64_t lda, int m, int k0, int w, int* piv,
-                        unsigned int* bar_count, cudaStream_t stream) {
+                        cudaStream_t stream) {
   const int rows = m - k0;
   const int max_smem = ctx->max_smem_optin;
   // CTAs: enough that each owns >= 32 rows, at most the SM count, and with
@@ -480,13 +751,8 @@ static int launch_panel(luhot_ctx* ctx, T* a, int64_t lda, int m, int k0, int w,
   args.rows_per = rows_per;
   args.lds = w + 1;
   args.piv = piv;
-  T* scratch = reinterpret_cast<T*>(ctx->panel_scratch);
-  args.cand_val = scratch;
-  args.cand_row = scratch + 2 * kMaxPanelCtas;
-  args.row_ul = args.cand_row + 2 * (size_t)kMaxPanelCtas * kMaxPanelWidth;
-  args.cand_idx = reinterpret_cast<int*>(args.row_ul + 2 * kMaxPanelWidth);
+  args.slots = static_cast<unsigned long long*>(ctx->panel_scratch);
   args.st = ctx->d_status;
-  args.bar_base = *bar_count;
   void* kargs[] = {&args};
   prof_begin(ctx, kProfPanel);
   LUHOT_CUDA_TRY(ctx, cudaLaunchCooperativeKernel((void*)kern, dim3(P), dim3(256), kargs, smem,
@@ -495,7 +761,6 @@ static int launch_panel(luhot_ctx* ctx, T* a, int64_t lda, int m, int k0, int w,
   double fl = 0.0;
   for (int j = 0; j < w; ++j) fl += (double)(rows - j - 1) * (1.0 + 2.0 * (w - j - 1));
   prof_end(ctx, kProfPanel, fl, 2.0 * rows * w * sizeof(T));
-  *bar_count += (unsigned int)P * (unsigned int)w;
   return LUHOT_OK;
 }
 
@@ -528,10 +793,12 @@ static int getrf_impl(luhot_ctx* ctx, int m, int n, T* a, int64_t lda, int* piv,
                       cudaStream_t stream, int tc_kind = -1, void* tc_a = nullptr, void* tc_b = nullptr,
                       float* tc_scal = nullptr) {
   const int dim_min = std::min(m, n);
-  unsigned int bar_count = 0;
+  // Exchange words carry step tags; clear them so no word of an earlier
+  // factorization carries a live tag.
+  LUHOT_CUDA_TRY(ctx, cudaMemsetAsync(ctx->panel_scratch, 0, kPanelScratchBytes, stream));
   for (int k0 = 0; k0 < dim_min; k0 += nb) {
     const int w = std::min(nb, dim_min - k0);
-    int rc = launch_panel<T, kExact>(ctx, a, lda, m, k0, w, piv, &bar_count, stream);
+    int rc = launch_panel<T, kExact>(ctx, a, lda, m, k0, w, piv, stream);
     if (rc != LUHOT_OK) return rc;
     const int c_right = k0 + w;
     const int ncols_swap = k0 + std::max(0, n - c_right);

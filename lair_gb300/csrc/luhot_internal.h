@@ -19,6 +19,12 @@ constexpr int kMaxPanelCtas = 256;     // >= SM count
 constexpr int kDefaultPanelWidth = 64; // FP64 / FP32 CUDA-core and DMMA paths
 constexpr int kTcPanelWidth = 128;     // tensor-core (tcgen05) Schur-update path
 constexpr int kMaxPanelWidth = 128;    // sizes the panel kernel's scratch
+// Panel exchange slots: per step parity and CTA, a 6-word header (pivot key,
+// row id, reciprocal) and the candidate row segment, in 8-byte words of
+// (payload, step tag), two words per FP64 value.
+constexpr int kPanelHeaderWords = 6;
+constexpr int kPanelSlotWords = kPanelHeaderWords + 2 * kMaxPanelWidth;
+constexpr size_t kPanelScratchBytes = 2 * (size_t)kMaxPanelCtas * kPanelSlotWords * sizeof(unsigned long long);
 
 // Grow-only device buffer.
 struct DevBuf {
