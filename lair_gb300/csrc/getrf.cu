@@ -711,6 +711,136 @@ __global__ void __launch_bounds__(256) gemm_dmma_kernel(double* a, int64_t lda, 
   }
 }
 
+// Persistent form of the same update for aligned operands: one CTA per SM
+// walks a contiguous range of 128 x 128 tiles in row-block order, so the
+// L21 block (A) changes only when the range crosses a row block.  The next
+// tile's U12 block (B) is copied into a second buffer by cp.async while the
+// current tile runs on the FP64 pipe, and the C tile is prefetched into L2
+// before its read-modify-write.  The FP64 pipe therefore stays busy across
+// tile boundaries instead of idling through each tile's loads and stores.
+// Needs 16-byte aligned rows and panel columns (even lda, kk0 and c0 and a
+// 16-byte aligned base); the launcher falls back to gemm_dmma_kernel.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem, int src_bytes) {
+  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+__global__ void __launch_bounds__(256, 1) gemm_dmma_persistent_kernel(double* a, int64_t lda, int r0, int c0,
+                                                                      int kk0, int K, int M, int N) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int Kpad = (K + 15) & ~15;
+  const int Kp = Kpad + 4;
+  const int ldb = kDmmaBN + 4;
+  double* As = reinterpret_cast<double*>(smem_raw);  // [128][Kp]
+  double* Bs0 = As + kDmmaBM * Kp;                   // [2][Kpad][ldb]
+  const int tiles_n = (N + kDmmaBN - 1) / kDmmaBN;
+  const int tiles = ((M + kDmmaBM - 1) / kDmmaBM) * tiles_n;
+  const int G = gridDim.x;
+  const int t_begin = (int)((int64_t)blockIdx.x * tiles / G);
+  const int t_end = (int)((int64_t)(blockIdx.x + 1) * tiles / G);
+  if (t_begin >= t_end) return;
+  const int tid = threadIdx.x;
+  const int lane = tid & 31, warp = tid >> 5;
+  const int wr = (warp >> 1) * 32, wc = (warp & 1) * 64;
+  const int g = lane >> 2, t4 = lane & 3;
+  const int kchunks = Kpad / 2;  // 16-byte chunks per A row
+
+  auto load_a = [&](int tm) {
+    const int tile_r = r0 + tm * kDmmaBM;
+    for (int idx = tid; idx < kDmmaBM * kchunks; idx += 256) {
+      const int i = idx / kchunks, k = (idx - i * kchunks) * 2;
+      const int r = tile_r + i;
+      const int valid = (r < r0 + M) ? max(0, min(2, K - k)) : 0;
+      const double* src = valid ? a + (int64_t)r * lda + kk0 + k : a;
+      cp_async16(As + i * Kp + k, src, valid * 8);
+    }
+  };
+  auto load_b = [&](int tn, double* Bs) {
+    const int tile_c = c0 + tn * kDmmaBN;
+    for (int idx = tid; idx < Kpad * (kDmmaBN / 2); idx += 256) {
+      const int k = idx / (kDmmaBN / 2), j = (idx - k * (kDmmaBN / 2)) * 2;
+      const int c = tile_c + j;
+      const int valid = (k < K) ? max(0, min(2, c0 + N - c)) : 0;
+      const double* src = valid ? a + (int64_t)(kk0 + k) * lda + c : a;
+      cp_async16(Bs + k * ldb + j, src, valid * 8);
+    }
+  };
+
+  int tm = t_begin / tiles_n, tn = t_begin - tm * tiles_n;
+  load_a(tm);
+  load_b(tn, Bs0);
+  cp_async_commit();
+  for (int t = t_begin; t < t_end; ++t) {
+    double* Bs = Bs0 + (size_t)((t - t_begin) & 1) * Kpad * ldb;
+    cp_async_wait_all();
+    __syncthreads();
+    const int tile_r = r0 + tm * kDmmaBM, tile_c = c0 + tn * kDmmaBN;
+    // Next tile: its B block now (other buffer, last read two tiles ago).
+    int tm_n = tm, tn_n = tn + 1;
+    if (tn_n == tiles_n) {
+      tn_n = 0;
+      ++tm_n;
+    }
+    const bool more = t + 1 < t_end;
+    if (more) {
+      load_b(tn_n, Bs0 + (size_t)((t + 1 - t_begin) & 1) * Kpad * ldb);
+      cp_async_commit();
+    }
+    // C tile into L2 ahead of its read-modify-write: 128 rows x 1 KB.
+    for (int idx = tid; idx < kDmmaBM * 8; idx += 256) {
+      const int i = idx >> 3, part = idx & 7;
+      const int r = tile_r + i, c = tile_c + part * 16;
+      if (r < r0 + M && c < c0 + N) asm volatile("prefetch.global.L2 [%0];" ::"l"(a + (int64_t)r * lda + c));
+    }
+    double acc[4][8][2];
+#pragma unroll
+    for (int mi = 0; mi < 4; ++mi)
+#pragma unroll
+      for (int ni = 0; ni < 8; ++ni) acc[mi][ni][0] = acc[mi][ni][1] = 0.0;
+    const int Kmma = (K + 3) & ~3;
+    for (int k = 0; k < Kmma; k += 4) {
+      double af[4], bf[8];
+#pragma unroll
+      for (int mi = 0; mi < 4; ++mi) af[mi] = As[(wr + mi * 8 + g) * Kp + k + t4];
+#pragma unroll
+      for (int ni = 0; ni < 8; ++ni) bf[ni] = Bs[(k + t4) * ldb + wc + ni * 8 + g];
+#pragma unroll
+      for (int mi = 0; mi < 4; ++mi)
+#pragma unroll
+        for (int ni = 0; ni < 8; ++ni) dmma_8x8x4(acc[mi][ni][0], acc[mi][ni][1], af[mi], bf[ni]);
+    }
+    if (more && tm_n != tm) {
+      // The range crosses into the next row block: reload A once every warp
+      // is done with it.
+      __syncthreads();
+      load_a(tm_n);
+      cp_async_commit();
+    }
+#pragma unroll
+    for (int mi = 0; mi < 4; ++mi) {
+      const int r = tile_r + wr + mi * 8 + g;
+      if (r >= r0 + M) continue;
+#pragma unroll
+      for (int ni = 0; ni < 8; ++ni) {
+        const int c = tile_c + wc + ni * 8 + t4 * 2;
+        double* dst = a + (int64_t)r * lda + c;
+        if (c + 1 < c0 + N) {
+          double2 v = *reinterpret_cast<double2*>(dst);
+          v.x -= acc[mi][ni][0];
+          v.y -= acc[mi][ni][1];
+          *reinterpret_cast<double2*>(dst) = v;
+        } else if (c < c0 + N) {
+          dst[0] -= acc[mi][ni][0];
+        }
+      }
+    }
+    tm = tm_n;
+    tn = tn_n;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Host driver.
 // ---------------------------------------------------------------------------
@@ -771,11 +901,23 @@ static int launch_gemm(luhot_ctx* ctx, T* a, int64_t lda, int r0, int c0, int kk
   if constexpr (std::is_same<T, double>::value && !kExact) {
     const int Kpad = (K + 15) & ~15;
     const size_t smem = ((size_t)kDmmaBM * (Kpad + 4) + (size_t)Kpad * (kDmmaBN + 4)) * sizeof(double);
-    LUHOT_CUDA_TRY(ctx, cudaFuncSetAttribute(gemm_dmma_kernel,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    dim3 grid((N + kDmmaBN - 1) / kDmmaBN, (M + kDmmaBM - 1) / kDmmaBM);
-    prof_begin(ctx, kProfGemm);
-    gemm_dmma_kernel<<<grid, 256, smem, stream>>>(a, lda, r0, c0, kk0, K, M, N);
+    const size_t smem_p = smem + (size_t)Kpad * (kDmmaBN + 4) * sizeof(double);
+    const int tiles = ((N + kDmmaBN - 1) / kDmmaBN) * ((M + kDmmaBM - 1) / kDmmaBM);
+    const bool aligned = (lda % 2 == 0) && (kk0 % 2 == 0) && (c0 % 2 == 0) &&
+                         (reinterpret_cast<uintptr_t>(a) % 16 == 0);
+    if (aligned && smem_p <= (size_t)ctx->max_smem_optin) {
+      LUHOT_CUDA_TRY(ctx, cudaFuncSetAttribute(gemm_dmma_persistent_kernel,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_p));
+      prof_begin(ctx, kProfGemm);
+      gemm_dmma_persistent_kernel<<<std::min(tiles, ctx->num_sms), 256, smem_p, stream>>>(a, lda, r0, c0, kk0, K,
+                                                                                          M, N);
+    } else {
+      LUHOT_CUDA_TRY(ctx, cudaFuncSetAttribute(gemm_dmma_kernel,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      dim3 grid((N + kDmmaBN - 1) / kDmmaBN, (M + kDmmaBM - 1) / kDmmaBM);
+      prof_begin(ctx, kProfGemm);
+      gemm_dmma_kernel<<<grid, 256, smem, stream>>>(a, lda, r0, c0, kk0, K, M, N);
+    }
   } else {
     dim3 grid((N + kGemmTile - 1) / kGemmTile, (M + kGemmTile - 1) / kGemmTile);
     prof_begin(ctx, kProfGemm);
