@@ -323,6 +323,278 @@ __global__ void __launch_bounds__(128) tc_gemm_x3_kernel(const __grid_constant__
 }
 
 // ---------------------------------------------------------------------------
+// Persistent, warp-specialised form (all kinds).  One CTA per SM walks a
+// contiguous range of 128 x 128 tiles.  Six warps:
+//   warp 0      TMA producer: per tile and 128-byte K box, the A and B boxes
+//               (three pieces each for kTcBF16x3) into a ring of stages;
+//   warp 1      TMEM owner and MMA issuer: two 128-column FP32 accumulators,
+//               so one tile's MMAs overlap the previous tile's epilogue;
+//   warps 2-5   epilogue: tcgen05.ld of their 32 TMEM lanes, scale by alpha,
+//               stage 128 x 32 FP32 blocks in shared memory (128-byte
+//               swizzle) and add them into C with TMA reduce-add, so C is
+//               never read by the SM and its HBM traffic streams behind the
+//               tensor cores.
+// Stage ring: full[s] (TMA bytes landed) / empty[s] (MMAs that read the stage
+// completed, via tcgen05.commit); accumulators: tfull[b] / tempty[b].  All
+// mbarrier waits are bounded; on expiry a role records the error, raises the
+// abort flag and stops, and before exit the CTA waits (bounded) for its
+// copies and MMAs in flight and for its reductions to read their staging.
+// ---------------------------------------------------------------------------
+constexpr int kTcEpiWarps = 4;
+constexpr int kTcThreads = 64 + 32 * kTcEpiWarps;
+
+template <int KIND>
+struct TcShape {
+  static constexpr int kPieces = KIND == kTcBF16x3 ? 3 : 1;
+  static constexpr int kES = KIND == kTcTF32 ? 4 : 2;
+  static constexpr int kKBox = 128 / kES;
+  static constexpr int kStageBytes = 2 * kPieces * 16384;
+  static constexpr int kStages = KIND == kTcBF16x3 ? 2 : 4;
+  static constexpr int kStagingBytes = 2 * 16384;
+  static constexpr size_t kSmem = 1024 + (size_t)kStages * kStageBytes + kStagingBytes;
+};
+
+__device__ __forceinline__ void mbar_arrive(unsigned bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void tc_abort(DeviceStatus* st, int* s_abort) {
+  atomicCAS(&st->error, kDevOk, kDevBarrierTimeout);
+  atomicExch(&st->abort, 1);
+  atomicExch(s_abort, 1);
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(kTcThreads, 1)
+    tc_gemm_persistent_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                              const __grid_constant__ CUtensorMap tmC, int M, int N, int kalloc,
+                              const float* alpha_ptr, DeviceStatus* st) {
+  using Sh = TcShape<KIND>;
+  constexpr int S = Sh::kStages;
+  constexpr int PIECES = Sh::kPieces;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  unsigned char* ring = base;
+  unsigned char* staging = base + (size_t)S * Sh::kStageBytes;
+  __shared__ __align__(8) unsigned long long full[S], empty[S], tfull[2], tempty[2];
+  __shared__ unsigned tmem_base;
+  __shared__ int s_abort, s_issued, s_consumed, s_epi_stop;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const unsigned long long limit = st->timeout_ns;
+  const int tiles_n = (N + 127) / 128;
+  const int tiles = ((M + 127) / 128) * tiles_n;
+  const int G = gridDim.x;
+  const int t_begin = (int)((int64_t)blockIdx.x * tiles / G);
+  const int t_end = (int)((int64_t)(blockIdx.x + 1) * tiles / G);
+  const int nkb = kalloc / Sh::kKBox;
+
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(smem_u32(&tmem_base)));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < S; ++i) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&full[i])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&empty[i])));
+    }
+    for (int i = 0; i < 2; ++i) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&tfull[i])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&tempty[i])), "r"(kTcEpiWarps));
+    }
+    s_abort = 0;
+    s_issued = 0;
+    s_consumed = 0;
+    s_epi_stop = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;");
+    asm volatile("fence.proxy.async.shared::cta;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const unsigned tmem = tmem_base;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // Producer.
+      int it = 0;
+      for (int t = t_begin; t < t_end && !s_abort; ++t) {
+        const int tm = t / tiles_n, tn = t - tm * tiles_n;
+        for (int kb = 0; kb < nkb; ++kb, ++it) {
+          const int s = it % S;
+          if (!mbar_wait(smem_u32(&empty[s]), (unsigned)((it / S) & 1) ^ 1u, limit)) {
+            tc_abort(st, &s_abort);
+            break;
+          }
+          unsigned char* sa = ring + (size_t)s * Sh::kStageBytes;
+          unsigned char* sb = sa + PIECES * 16384;
+          asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(&full[s])),
+                       "r"((unsigned)Sh::kStageBytes)
+                       : "memory");
+          for (int pc = 0; pc < PIECES; ++pc) {
+            const int x = pc * kalloc + kb * Sh::kKBox;
+            asm volatile(
+                "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+                "[%4];" ::"r"(smem_u32(sa + pc * 16384)),
+                "l"(&tmA), "r"(x), "r"(tm * 128), "r"(smem_u32(&full[s]))
+                : "memory");
+            asm volatile(
+                "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+                "[%4];" ::"r"(smem_u32(sb + pc * 16384)),
+                "l"(&tmB), "r"(x), "r"(tn * 128), "r"(smem_u32(&full[s]))
+                : "memory");
+          }
+          s_issued = it + 1;
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // MMA issuer.
+      constexpr unsigned fmt = KIND == kTcTF32 ? 2u : ((KIND == kTcBF16 || KIND == kTcBF16x3) ? 1u : 0u);
+      constexpr unsigned idesc = (1u << 4) | (fmt << 7) | (fmt << 10) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
+      constexpr int NPROD = KIND == kTcBF16x3 ? 6 : 1;
+      const int pa[6] = {0, 0, 1, 0, 1, 2}, pb[6] = {0, 1, 0, 2, 1, 0};
+      int it = 0, tc = 0;
+      for (int t = t_begin; t < t_end && !s_abort; ++t, ++tc) {
+        const int b = tc & 1;
+        if (!mbar_wait(smem_u32(&tempty[b]), (unsigned)((tc >> 1) & 1) ^ 1u, limit)) {
+          tc_abort(st, &s_abort);
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const unsigned acc_addr = tmem + (unsigned)(b * 128);
+        bool ok = true;
+        for (int kb = 0; kb < nkb; ++kb, ++it) {
+          const int s = it % S;
+          if (!mbar_wait(smem_u32(&full[s]), (unsigned)((it / S) & 1), limit)) {
+            ok = false;
+            break;
+          }
+          s_consumed = it + 1;
+          asm volatile("tcgen05.fence::after_thread_sync;");
+          unsigned char* sa = ring + (size_t)s * Sh::kStageBytes;
+          unsigned char* sb = sa + PIECES * 16384;
+          for (int ks = 0; ks < 4; ++ks) {
+            for (int pr = 0; pr < NPROD; ++pr) {
+              const unsigned long long da = sw128_desc(smem_u32(sa + pa[pr] * 16384 + ks * 32));
+              const unsigned long long db = sw128_desc(smem_u32(sb + pb[pr] * 16384 + ks * 32));
+              const unsigned accf = (kb > 0 || ks > 0 || pr > 0) ? 1u : 0u;
+              if (KIND == kTcTF32)
+                asm volatile(
+                    "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, "
+                    "p;\n}\n" ::"r"(acc_addr),
+                    "l"(da), "l"(db), "r"(idesc), "r"(accf));
+              else
+                asm volatile(
+                    "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, "
+                    "p;\n}\n" ::"r"(acc_addr),
+                    "l"(da), "l"(db), "r"(idesc), "r"(accf));
+            }
+          }
+          // The stage is free once these MMAs have read it.
+          asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                           smem_u32(&empty[s]))
+                       : "memory");
+        }
+        if (!ok) {
+          tc_abort(st, &s_abort);
+          break;
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                         smem_u32(&tfull[b]))
+                     : "memory");
+      }
+    }
+  } else {
+    // Epilogue: warp w reads TMEM lanes 32 * (w % 4) .. + 31 = tile rows.
+    const int quarter = warp & 3;
+    const int row = quarter * 32 + lane;
+    const bool leader = (warp == 2 && lane == 0);
+    const float alpha = *alpha_ptr;
+    int tc = 0, sbuf = 0;
+    for (int t = t_begin; t < t_end; ++t, ++tc) {
+      const int tm = t / tiles_n, tn = t - tm * tiles_n;
+      const int b = tc & 1;
+      const bool got = mbar_wait(smem_u32(&tfull[b]), (unsigned)((tc >> 1) & 1), limit);
+      // One decision for all four epilogue warps (they meet at named
+      // barriers below): any failed wait or an abort stops them together.
+      const bool all_got = __all_sync(0xffffffffu, got);
+      if (lane == 0 && (!all_got || s_abort)) s_epi_stop = 1;
+      __syncwarp();
+      asm volatile("bar.sync 1, %0;" ::"n"(32 * kTcEpiWarps) : "memory");
+      if (s_epi_stop) {
+        if (leader) tc_abort(st, &s_abort);
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      for (int cb = 0; cb < 4; ++cb, sbuf ^= 1) {
+        unsigned r[32];
+        const unsigned taddr = tmem + ((unsigned)(quarter * 32) << 16) + (unsigned)(b * 128 + cb * 32);
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,"
+            "%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+              "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+              "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+            : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;");
+        if (cb == 3) {
+          // This warp is done with the accumulator: the MMA warp may reuse it.
+          asm volatile("tcgen05.fence::before_thread_sync;");
+          __syncwarp();
+          if (lane == 0) mbar_arrive(smem_u32(&tempty[b]));
+        }
+        // The staging block written two reductions ago must have been read.
+        if (leader) asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+        asm volatile("bar.sync 1, %0;" ::"n"(32 * kTcEpiWarps));
+        unsigned char* blk = staging + sbuf * 16384 + row * 128;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          float4 v;
+          v.x = alpha * __uint_as_float(r[4 * q + 0]);
+          v.y = alpha * __uint_as_float(r[4 * q + 1]);
+          v.z = alpha * __uint_as_float(r[4 * q + 2]);
+          v.w = alpha * __uint_as_float(r[4 * q + 3]);
+          *reinterpret_cast<float4*>(blk + ((q ^ (row & 7)) << 4)) = v;
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("bar.sync 1, %0;" ::"n"(32 * kTcEpiWarps));
+        if (leader) {
+          // Boxes past the last column are not issued; the (possibly empty)
+          // group is committed either way so the staging rotation stays in
+          // step with the groups.
+          if (tn * 128 + cb * 32 < N)
+            asm volatile(
+                "cp.reduce.async.bulk.tensor.2d.global.shared::cta.add.tile.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
+                    &tmC),
+                "r"(tn * 128 + cb * 32), "r"(tm * 128), "r"(smem_u32(staging + sbuf * 16384))
+                : "memory");
+          asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+        }
+      }
+    }
+    if (leader) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && s_abort) {
+    // Copies still in flight (issued, never consumed) must land before exit.
+    for (int i = s_consumed; i < s_issued; ++i) mbar_wait(smem_u32(&full[i % S]), (unsigned)((i / S) & 1), limit);
+  }
+  if (threadIdx.x == 32 && s_abort) {
+    // MMAs still running: every stage's last commit has arrived once they end.
+    for (int i = 0; i < S; ++i) {
+      const int uses = s_consumed - i > 0 ? (s_consumed - i + S - 1) / S : 0;
+      if (uses > 0) mbar_wait(smem_u32(&empty[i]), (unsigned)((uses - 1) & 1), limit);
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem));
+}
+
+// ---------------------------------------------------------------------------
 // Per-panel operand conversion.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void atomic_max_f32_nonneg(float* addr, float v) {
@@ -480,6 +752,22 @@ static int make_map(luhot_ctx* ctx, CUtensorMap* m, void* ptr, int kind, int row
   return LUHOT_OK;
 }
 
+// C (M x N FP32, row stride ldc) as the target of 128-row x 32-column
+// reduce-add boxes, 128-byte swizzled like the staging blocks.
+static int make_c_map(luhot_ctx* ctx, CUtensorMap* m, float* c, int M, int N, int64_t ldc) {
+  EncodeTiledFn enc = encode_fn();
+  if (!enc) return set_error(ctx, LUHOT_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled is unavailable");
+  cuuint64_t dims[2] = {(cuuint64_t)N, (cuuint64_t)M};
+  cuuint64_t strides[1] = {(cuuint64_t)ldc * 4};
+  cuuint32_t box[2] = {32, 128};
+  cuuint32_t estr[2] = {1, 1};
+  const CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, c, dims, strides, box, estr,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return set_error(ctx, LUHOT_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+  return LUHOT_OK;
+}
+
 template <int KIND>
 static int launch_tc(luhot_ctx* ctx, float* a, int64_t lda, int k0, int w, int m, int n, void* aop, void* bop,
                      float* scal, cudaStream_t stream) {
@@ -506,13 +794,28 @@ static int launch_tc(luhot_ctx* ctx, float* a, int64_t lda, int k0, int w, int m
   if (rc) return rc;
   rc = make_map(ctx, &tB, bop, KIND, N, kalloc);
   if (rc) return rc;
-  const int kbox = KIND == kTcTF32 ? 32 : 64;
-  const size_t smem = KIND == kTcBF16x3 ? 1024 + 6 * 16384 : 1024 + (size_t)(kalloc / kbox) * 2 * 16384;
-  auto kern = KIND == kTcBF16x3 ? tc_gemm_x3_kernel : tc_gemm_kernel<KIND>;
-  LUHOT_CUDA_TRY(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  dim3 grid((N + 127) / 128, (M + 127) / 128);
-  prof_begin(ctx, kProfGemm);
-  kern<<<grid, 128, smem, stream>>>(tA, tB, a + (int64_t)r1 * lda + c1, lda, M, N, w, scal + 4, ctx->d_status);
+  float* cbase = a + (int64_t)r1 * lda + c1;
+  const bool c_aligned = (lda % 4 == 0) && (reinterpret_cast<uintptr_t>(cbase) % 16 == 0);
+  if (c_aligned && TcShape<KIND>::kSmem <= (size_t)ctx->max_smem_optin) {
+    CUtensorMap tC;
+    rc = make_c_map(ctx, &tC, cbase, M, N, lda);
+    if (rc) return rc;
+    auto kern = tc_gemm_persistent_kernel<KIND>;
+    LUHOT_CUDA_TRY(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)TcShape<KIND>::kSmem));
+    const int tiles = ((M + 127) / 128) * ((N + 127) / 128);
+    prof_begin(ctx, kProfGemm);
+    kern<<<std::min(tiles, ctx->num_sms), kTcThreads, TcShape<KIND>::kSmem, stream>>>(tA, tB, tC, M, N, kalloc,
+                                                                                    scal + 4, ctx->d_status);
+  } else {
+    const int kbox = KIND == kTcTF32 ? 32 : 64;
+    const size_t smem = KIND == kTcBF16x3 ? 1024 + 6 * 16384 : 1024 + (size_t)(kalloc / kbox) * 2 * 16384;
+    auto kern = KIND == kTcBF16x3 ? tc_gemm_x3_kernel : tc_gemm_kernel<KIND>;
+    LUHOT_CUDA_TRY(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 grid((N + 127) / 128, (M + 127) / 128);
+    prof_begin(ctx, kProfGemm);
+    kern<<<grid, 128, smem, stream>>>(tA, tB, cbase, lda, M, N, w, scal + 4, ctx->d_status);
+  }
   prof_end(ctx, kProfGemm, 2.0 * M * (double)N * w,
            8.0 * M * (double)N + (double)(M + N) * kalloc * (KIND == kTcTF32 ? 4 : KIND == kTcBF16x3 ? 6 : 2));
   LUHOT_CUDA_TRY(ctx, cudaGetLastError());
