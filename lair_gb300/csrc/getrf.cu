@@ -568,6 +568,52 @@ __global__ void __launch_bounds__(kTrsmCols) trsm_kernel(T* a, int64_t lda, int 
   for (int i = 1; i < w; ++i) a[(int64_t)(k0 + i) * lda + c] = X[i * kTrsmCols + tid];
 }
 
+// Fast-mode U12 solve, left-looking in blocks of 16 rows: one thread per
+// column; for rows i0..i0+15 it accumulates x_i = b_i - sum_{k<i0} l_ik x_k
+// in 16 registers (16 independent FMA chains per loaded x_k, the l_ik
+// broadcast from shared memory with L11 stored transposed), then solves the
+// 16 x 16 diagonal block.  x lives in shared memory (one column per thread,
+// conflict-free).  W = 64 or 128 >= w; L11 is zero-padded to W x W.  The
+// exact mode keeps trsm_kernel's order.
+template <typename T, int W>
+__global__ void __launch_bounds__(kTrsmCols) trsm_fast_kernel(T* a, int64_t lda, int k0, int w, int c0, int n) {
+  constexpr int RB = 16;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* Lt = reinterpret_cast<T*>(smem_raw);  // [W][W]: Lt[k][i] = L11[i][k] for i > k, else 0
+  T* X = Lt + W * W;                       // [W][kTrsmCols]
+  const int tid = threadIdx.x;
+  for (int idx = tid; idx < W * W; idx += blockDim.x) {
+    const int k = idx / W, i = idx - k * W;
+    Lt[idx] = (i > k && i < w && k < w) ? a[(int64_t)(k0 + i) * lda + k0 + k] : T(0);
+  }
+  const int c = c0 + blockIdx.x * kTrsmCols + tid;
+  const bool active = c < n;
+  for (int i = 0; i < W; ++i) X[i * kTrsmCols + tid] = (active && i < w) ? a[(int64_t)(k0 + i) * lda + c] : T(0);
+  __syncthreads();
+  for (int i0 = 0; i0 < w; i0 += RB) {
+    T acc[RB];
+#pragma unroll
+    for (int r = 0; r < RB; ++r) acc[r] = X[(i0 + r) * kTrsmCols + tid];
+    for (int k = 0; k < i0; ++k) {
+      const T xk = X[k * kTrsmCols + tid];
+      const T* lk = Lt + k * W + i0;
+#pragma unroll
+      for (int r = 0; r < RB; ++r) acc[r] = fma(-lk[r], xk, acc[r]);
+    }
+#pragma unroll
+    for (int kk = 0; kk < RB - 1; ++kk) {
+      const T* lk = Lt + (i0 + kk) * W + i0;
+#pragma unroll
+      for (int r = 0; r < RB; ++r)
+        if (r > kk) acc[r] = fma(-lk[r], acc[kk], acc[r]);
+    }
+#pragma unroll
+    for (int r = 0; r < RB; ++r) X[(i0 + r) * kTrsmCols + tid] = acc[r];
+  }
+  if (active)
+    for (int i = 1; i < w; ++i) a[(int64_t)(k0 + i) * lda + c] = X[i * kTrsmCols + tid];
+}
+
 // ---------------------------------------------------------------------------
 // 4a. Schur update on the CUDA cores (exact mode and FP32): C -= A B with a
 //     64x64 tile per CTA, 4x4 per thread, K <= 64 staged in shared memory.
@@ -854,9 +900,13 @@ static int launch_panel(luhot_ctx* ctx, T* a, int64_t lda, int m, int k0, int w,
                         cudaStream_t stream) {
   const int rows = m - k0;
   const int max_smem = ctx->max_smem_optin;
-  // CTAs: enough that each owns >= 32 rows, at most the SM count, and with
-  // the rows of one CTA fitting in shared memory.
-  int P = std::min(ctx->num_sms, std::max(1, (rows + 31) / 32));
+  // CTAs: enough that each owns >= 32 rows, at most pmax (raised up to the
+  // SM count when the rows of one CTA would not fit in shared memory).
+  // The exchange latency per column grows with P; FP32 panels (whose
+  // update work is light) run fastest on 64 CTAs, FP64 panels need the
+  // FP64 pipes of every SM.
+  const int pmax = sizeof(T) == 4 ? std::min(ctx->num_sms, 64) : ctx->num_sms;
+  int P = std::min(pmax, std::max(1, (rows + 31) / 32));
   int rows_per = (rows + P - 1) / P;
   while (panel_smem_bytes<T>(rows_per, w) > (size_t)max_smem && P < ctx->num_sms) {
     P = std::min(ctx->num_sms, P * 2);
@@ -952,13 +1002,27 @@ static int getrf_impl(luhot_ctx* ctx, int m, int n, T* a, int64_t lda, int* piv,
       LUHOT_CUDA_TRY(ctx, cudaGetLastError());
     }
     if (c_right < n) {
-      const size_t smem = ((size_t)w * w + (size_t)w * kTrsmCols) * sizeof(T);
-      auto kern = trsm_kernel<T, kExact>;
-      LUHOT_CUDA_TRY(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               (int)smem));
+      const int tgrid = (n - c_right + kTrsmCols - 1) / kTrsmCols;
       prof_begin(ctx, kProfTrsm);
-      kern<<<(n - c_right + kTrsmCols - 1) / kTrsmCols, kTrsmCols, smem, stream>>>(a, lda, k0, w,
-                                                                                   c_right, n);
+      if (!kExact && w <= 64) {
+        const size_t smem = ((size_t)64 * 64 + (size_t)64 * kTrsmCols) * sizeof(T);
+        LUHOT_CUDA_TRY(ctx, cudaFuncSetAttribute(trsm_fast_kernel<T, 64>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        trsm_fast_kernel<T, 64><<<tgrid, kTrsmCols, smem, stream>>>(a, lda, k0, w, c_right, n);
+      } else if (!kExact && std::is_same<T, float>::value && w <= 128) {
+        if constexpr (std::is_same<T, float>::value) {
+          const size_t smem = ((size_t)128 * 128 + (size_t)128 * kTrsmCols) * sizeof(T);
+          LUHOT_CUDA_TRY(ctx, cudaFuncSetAttribute(trsm_fast_kernel<T, 128>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+          trsm_fast_kernel<T, 128><<<tgrid, kTrsmCols, smem, stream>>>(a, lda, k0, w, c_right, n);
+        }
+      } else {
+        const size_t smem = ((size_t)w * w + (size_t)w * kTrsmCols) * sizeof(T);
+        auto kern = trsm_kernel<T, kExact>;
+        LUHOT_CUDA_TRY(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)smem));
+        kern<<<tgrid, kTrsmCols, smem, stream>>>(a, lda, k0, w, c_right, n);
+      }
       prof_end(ctx, kProfTrsm, (double)w * (w - 1) * (n - c_right),
                ((double)w * w + 2.0 * w * (n - c_right)) * sizeof(T));
       LUHOT_CUDA_TRY(ctx, cudaGetLastError());
