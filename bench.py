@@ -280,11 +280,11 @@ def run_ours(args):
 
     g = prof.get("gemm", {"ms": 0.0, "flops": 0.0, "launches": 0})
     gemm_tflops = g["flops"] / (g["ms"] * 1e-3) / 1e12 if g["ms"] else 0.0
-    traffic = read_traffic(os.path.join(ROOT, "profiles", "gemm_dmma_fp64_n16384.md"))
+    traffic = read_traffic(os.path.join(ROOT, "profiles", "gemm_dmma_persistent_fp64_n16384.md"))
     total_prof_ms = sum(v["ms"] for v in prof.values())
     roofline = {"bound": "tensor", "achieved": gemm_tflops, "peak": peak, "unit": "TFLOP/s",
                 "frac": gemm_tflops / peak if peak else None, "traffic": traffic,
-                "kernel": "gemm_dmma_kernel (FP64 Schur update, mma.sync m8n8k4)",
+                "kernel": "gemm_dmma_persistent_kernel (FP64 Schur update, mma.sync m8n8k4)",
                 "peak_source": "FP64 DMMA throughput measured in this run (register-resident "
                                "mma.sync m8n8k4 loop); MEASURED_PEAKS.json has no FP64 figure",
                 "per_launch_flops": g["flops"] / max(1, g["launches"]),
@@ -358,8 +358,18 @@ def conditioned_system(n, kappa, seed, torch):
     values only relatively, so kappa is kept), sigma geometric 1 -> 1/kappa,
     product formed in FP64; b iid N(0,1)."""
     gen = torch.Generator(device="cuda").manual_seed(seed)
-    q1, _ = torch.linalg.qr(torch.randn((n, n), device="cuda", generator=gen))
-    q2, _ = torch.linalg.qr(torch.randn((n, n), device="cuda", generator=gen))
+    g1 = torch.randn((n, n), device="cuda", generator=gen)
+    g2 = torch.randn((n, n), device="cuda", generator=gen)
+    try:
+        q1, _ = torch.linalg.qr(g1)
+        q2, _ = torch.linalg.qr(g2)
+    except RuntimeError:
+        # torch's GPU linear-algebra library cannot always be loaded (e.g.
+        # under a profiler's injection); the same seeded matrices then go
+        # through LAPACK on the host.
+        q1 = torch.from_numpy(np.linalg.qr(g1.cpu().numpy())[0]).cuda()
+        q2 = torch.from_numpy(np.linalg.qr(g2.cpu().numpy())[0]).cuda()
+    del g1, g2
     sigma = torch.logspace(0, -float(np.log10(kappa)), n, dtype=torch.float64, device="cuda")
     a = (q1.double() * sigma) @ q2.double().T
     del q1, q2
