@@ -266,6 +266,10 @@ static int getrf_host(luhot_ctx* ctx, int64_t m, int64_t n, T* a, int64_t rs, in
     return set_error(ctx, LUHOT_ERR_INVALID_ARG, "getrf: null pointer");
   if (singular) *singular = -1;
   if (k == 0) return LUHOT_OK;
+  // lair factors non-standard layouts with its column-major (Crout) order
+  // (src/lapack/getrf.rs:22-26); exact mode follows it bit for bit.
+  if (mode == LUHOT_MODE_EXACT && getrf_uses_colmajor(m, n, rs, cs))
+    return getrf_colmajor_host<T>(ctx, m, n, a, rs, cs, piv, singular);
   const int64_t lda = dev_ld<T>(n);
   int rc = ensure_buf(ctx, ctx->work[0], (size_t)m * lda * sizeof(T));
   if (rc) return rc;

@@ -112,6 +112,13 @@ int gesv_ir_device(luhot_ctx* ctx, int n, int nrhs, const double* a, int64_t lda
                    double* x, int64_t ldx, int precision, int solver, double tol, int max_iter,
                    luhot_ir_info* info);
 
+// lair's getrf_col_major order (non-standard layouts, exact mode): true when
+// the array is not in ndarray's standard layout and has at most 4096 rows.
+bool getrf_uses_colmajor(int64_t m, int64_t n, int64_t rs, int64_t cs);
+template <typename T>
+int getrf_colmajor_host(luhot_ctx* ctx, int64_t m, int64_t n, T* a, int64_t rs, int64_t cs, uint64_t* piv,
+                        int64_t* singular);
+
 template <typename T>
 int getrs_device(luhot_ctx* ctx, int n, int nrhs, const T* lu, int64_t lda, const int* piv,
                  const T* b, int64_t ldb, T* x, int64_t ldx, int trans, int mode);
