@@ -68,6 +68,18 @@ def lib():
         L.oracle_dgemv_notrans.argtypes = [_i64, _i64, ctypes.c_double, _vp, _i64, _i64, _vp, _i64,
                                            ctypes.c_double, _vp, _i64]
         L.oracle_dgemv_notrans.restype = None
+        for name in ("oracle_dgeqrf", "oracle_sgeqrf"):
+            getattr(L, name).argtypes = [_i64, _i64, _vp, _i64, _i64, _vp]
+            getattr(L, name).restype = None
+        for name in ("oracle_dqr_q", "oracle_sqr_q"):
+            getattr(L, name).argtypes = [_i64, _i64, _vp, _i64, _i64, _vp, _i64, _vp]
+            getattr(L, name).restype = None
+        L.oracle_dlarfg.argtypes = [ctypes.c_double, _i64, _vp, _i64, _vp, _vp]
+        L.oracle_dlarfg.restype = None
+        L.oracle_dlarf_left.argtypes = [_i64, _i64, _vp, _i64, ctypes.c_double, _vp, _i64, _i64]
+        L.oracle_dlarf_left.restype = None
+        L.oracle_dnrm2.argtypes = [_i64, _vp, _i64]
+        L.oracle_dnrm2.restype = ctypes.c_double
         _lib = L
     return _lib
 
@@ -187,3 +199,52 @@ def getrs_multi(lu: np.ndarray, piv, B: np.ndarray) -> np.ndarray:
 
 def dot(x: np.ndarray, y: np.ndarray, n: int) -> float:
     return lib().oracle_ddot(n, _ptr(x), _estrides(x)[0], _ptr(y), _estrides(y)[0])
+
+
+# ------------------------------------------------------------------- QR
+def geqrf(a: np.ndarray) -> np.ndarray:
+    """src/lapack/geqrf.rs:9-27: Householder QR of ``a`` in place; returns tau."""
+    p = _prefix(a)
+    m, n = a.shape
+    rs, cs = _estrides(a)
+    tau = np.zeros(min(m, n), dtype=a.dtype)
+    getattr(lib(), f"oracle_{p}geqrf")(m, n, _ptr(a), rs, cs, _ptr(tau))
+    return tau
+
+
+def qr_q(qr: np.ndarray, tau: np.ndarray) -> np.ndarray:
+    """src/decomposition/qr.rs:26-60: Q (m x m) from the factored array and tau."""
+    p = _prefix(qr)
+    m, n = qr.shape
+    rs, cs = _estrides(qr)
+    t = np.ascontiguousarray(tau, dtype=qr.dtype)
+    q = np.zeros((m, m), dtype=qr.dtype)
+    getattr(lib(), f"oracle_{p}qr_q")(m, n, _ptr(qr), rs, cs, _ptr(t), t.shape[0], _ptr(q))
+    return q
+
+
+def qr_r(qr: np.ndarray) -> np.ndarray:
+    """src/decomposition/qr.rs:63-72: the array with its strictly lower part zeroed."""
+    r = qr.copy()
+    for i in range(1, r.shape[0]):
+        r[i, : min(i, r.shape[1])] = 0
+    return r
+
+
+def larfg(alpha: float, x: np.ndarray):
+    """src/lapack/larfg.rs:9-43 (float64): scales x in place; returns (beta, tau)."""
+    beta = np.zeros(1)
+    tau = np.zeros(1)
+    lib().oracle_dlarfg(alpha, x.shape[0], _ptr(x), _estrides(x)[0] if x.size else 1, _ptr(beta), _ptr(tau))
+    return float(beta[0]), float(tau[0])
+
+
+def larf_left(v: np.ndarray, tau: float, c: np.ndarray) -> None:
+    """src/lapack/larf.rs:10-52 (float64): c <- (I - tau v v^T) c in place."""
+    rs, cs = _estrides(c)
+    lib().oracle_dlarf_left(c.shape[0], c.shape[1], _ptr(v), _estrides(v)[0], tau, _ptr(c), rs, cs)
+
+
+def nrm2(x: np.ndarray) -> float:
+    """src/blas/nrm2.rs:6-15 (float64)."""
+    return float(lib().oracle_dnrm2(x.shape[0], _ptr(x), _estrides(x)[0] if x.size else 1))

@@ -324,6 +324,158 @@ void getrs(int64_t m, int64_t ncols, const T* lu, int64_t rs, int64_t cs, const 
 
 }  // namespace
 
+
+// ---------------------------------------------------------------------------
+// QR: lair's unblocked Householder geqrf and its helpers (real element types).
+// ---------------------------------------------------------------------------
+
+// src/scalar.rs:393-402: eps = epsilon / 2, sfmin = smallest positive normal.
+template <typename T>
+T lair_eps() {
+  return std::numeric_limits<T>::epsilon() / (T(1) + T(1));
+}
+template <typename T>
+T lair_sfmin() {
+  return std::numeric_limits<T>::min();
+}
+
+// Rust's powi (LLVM's powi by repeated squaring, compiler-rt __powidf2 order).
+template <typename T>
+T powi(T a, int b) {
+  const bool recip = b < 0;
+  T r = T(1);
+  for (;;) {
+    if (b & 1) r *= a;
+    b /= 2;
+    if (b == 0) break;
+    a *= a;
+  }
+  return recip ? T(1) / r : r;
+}
+
+// src/blas/nrm2.rs:6-15: sqrt of the sequential sum of v*v (+ im*im = 0).
+template <typename T>
+T nrm2(int64_t n, const T* x, int64_t inc) {
+  T sum = -T(0);  // Rust's float Sum folds from -0.0
+  for (int64_t i = 0; i < n; ++i) {
+    const T v = x[i * inc];
+    sum = sum + (v * v + T(0) * T(0));
+  }
+  return std::sqrt(sum);
+}
+
+// src/lapack.rs:63-65
+template <typename T>
+T lapy3(T x, T y, T z) {
+  return std::sqrt(x * x + y * y + z * z);
+}
+
+// src/lapack/larfg.rs:9-43 (real alpha): scales x in place, returns beta and tau.
+template <typename T>
+void larfg(T alpha, int64_t n, T* x, int64_t inc, T* beta_out, T* tau_out) {
+  T x_norm = nrm2<T>(n, x, inc);
+  if (x_norm == T(0)) {  // alpha.im() == 0 for real types
+    *beta_out = alpha;
+    *tau_out = T(0);
+    return;
+  }
+  T beta = -std::copysign(lapy3<T>(alpha, T(0), x_norm), alpha);
+  const T safe_min = lair_sfmin<T>() / lair_eps<T>();
+  int knt = 0;
+  if (std::fabs(beta) < safe_min) {
+    const T safe_min_recip = T(1) / safe_min;
+    for (;;) {
+      ++knt;
+      for (int64_t i = 0; i < n; ++i) x[i * inc] *= safe_min_recip;
+      beta *= safe_min_recip;
+      alpha *= safe_min_recip;
+      if (std::fabs(beta) >= safe_min || knt >= 20) break;
+    }
+    x_norm = nrm2<T>(n, x, inc);
+    beta = -std::copysign(alpha * alpha + x_norm * x_norm, alpha);
+  }
+  const T tau = (beta - alpha) / beta;
+  alpha = T(1) / (alpha - beta);
+  for (int64_t i = 0; i < n; ++i) x[i * inc] *= alpha;
+  beta *= powi<T>(safe_min, knt);
+  *beta_out = beta;
+  *tau_out = tau;
+}
+
+// src/lapack/ilal.rs:6-22: last column with a non-zero entry, or -1.
+template <typename T>
+int64_t ilalc(int64_t rows, int64_t cols, const T* c, int64_t rs, int64_t cs) {
+  if (rows == 0 || cols == 0) return -1;
+  if (c[(rows - 1) * rs + (cols - 1) * cs] != T(0)) return cols - 1;
+  for (int64_t j = cols - 1; j >= 0; --j)
+    for (int64_t i = 0; i < rows; ++i)
+      if (c[i * rs + j * cs] != T(0)) return j;
+  return -1;
+}
+
+// src/lapack/larf.rs:10-52: C <- (I - tau v v^T) C via w = C^T v
+// (gemv::conjtrans, src/blas/gemv.rs:58-86) and C += (-tau v) w^T
+// (gerc, src/blas/gerc.rs).  v has m entries (C is m x n).
+template <typename T>
+void larf_left(int64_t m, int64_t n, const T* v, int64_t incv, T tau, T* c, int64_t rs, int64_t cs) {
+  if (tau == T(0)) return;
+  int64_t last_v = m - 1;
+  while (last_v >= 0 && v[last_v * incv] == T(0)) --last_v;  // lair unwraps: v has a non-zero
+  const int64_t last_c = ilalc<T>(last_v + 1, n, c, rs, cs);
+  if (last_c < 0) return;
+  std::vector<T> w((size_t)last_c + 1);
+  for (int64_t j = 0; j <= last_c; ++j) {
+    T sum = T(0);
+    for (int64_t i = 0; i <= last_v; ++i) sum = sum + c[i * rs + j * cs] * v[i * incv];
+    w[(size_t)j] = T(0) + T(1) * sum;
+  }
+  for (int64_t i = 0; i <= last_v; ++i) {
+    const T factor = -tau * v[i * incv];
+    for (int64_t j = 0; j <= last_c; ++j) c[i * rs + j * cs] += factor * w[(size_t)j];
+  }
+}
+
+// src/lapack/geqrf.rs:9-27
+template <typename T>
+void geqrf(int64_t m, int64_t n, T* a, int64_t rs, int64_t cs, T* tau) {
+  const int64_t k = std::min(m, n);
+  for (int64_t i = 0; i < k; ++i) {
+    T beta, t;
+    larfg<T>(a[i * rs + i * cs], m - i - 1, a + (i + 1) * rs + i * cs, rs, &beta, &t);
+    tau[i] = t;
+    a[i * rs + i * cs] = T(1);
+    std::vector<T> v((size_t)(m - i));
+    for (int64_t r = i; r < m; ++r) v[(size_t)(r - i)] = a[r * rs + i * cs];
+    larf_left<T>(m - i, n - i - 1, v.data(), 1, t, a + i * rs + (i + 1) * cs, rs, cs);
+    a[i * rs + i * cs] = beta;
+  }
+}
+
+// src/decomposition/qr.rs:26-60: Q (m x m, row-major) from the factored array and tau.
+template <typename T>
+void qr_q(int64_t m, int64_t n, const T* qr, int64_t rs, int64_t cs, const T* tau, int64_t ntau, T* q) {
+  for (int64_t i = 0; i < m * m; ++i) q[i] = T(0);
+  for (int64_t j = 0; j < ntau; ++j)
+    for (int64_t i = 0; i < m; ++i) q[i * m + j] = qr[i * rs + j * cs];
+  for (int64_t j = ntau; j < m; ++j) {
+    for (int64_t l = 0; l < m; ++l) q[l * m + j] = T(0);
+    q[j * m + j] = T(1);
+  }
+  for (int64_t i = ntau - 1; i >= 0; --i) {
+    if (i < m - 1) {
+      q[i * m + i] = T(1);
+      std::vector<T> v((size_t)(m - i));
+      for (int64_t r = i; r < m; ++r) v[(size_t)(r - i)] = q[r * m + i];
+      larf_left<T>(m - i, m - i - 1, v.data(), 1, tau[i], q + i * m + i + 1, m, 1);
+    }
+    if (i < m - 1)
+      for (int64_t r = i + 1; r < m; ++r) q[r * m + i] *= -tau[i];
+    q[i * m + i] = T(1) - tau[i];
+    for (int64_t l = 0; l < i; ++l) q[l * m + i] = T(0);
+  }
+  (void)n;
+}
+
 extern "C" {
 
 int oracle_is_standard_layout(int64_t m, int64_t n, int64_t rs, int64_t cs) {
@@ -405,5 +557,28 @@ void oracle_dgemv_notrans(int64_t m, int64_t n, double alpha, const double* a, i
                           int64_t incy) {
   gemv_notrans<double>(m, n, alpha, a, rs, cs, x, incx, beta, y, incy);
 }
+
+void oracle_dgeqrf(int64_t m, int64_t n, double* a, int64_t rs, int64_t cs, double* tau) {
+  geqrf<double>(m, n, a, rs, cs, tau);
+}
+void oracle_sgeqrf(int64_t m, int64_t n, float* a, int64_t rs, int64_t cs, float* tau) {
+  geqrf<float>(m, n, a, rs, cs, tau);
+}
+void oracle_dqr_q(int64_t m, int64_t n, const double* qr, int64_t rs, int64_t cs, const double* tau,
+                  int64_t ntau, double* q) {
+  qr_q<double>(m, n, qr, rs, cs, tau, ntau, q);
+}
+void oracle_sqr_q(int64_t m, int64_t n, const float* qr, int64_t rs, int64_t cs, const float* tau,
+                  int64_t ntau, float* q) {
+  qr_q<float>(m, n, qr, rs, cs, tau, ntau, q);
+}
+void oracle_dlarfg(double alpha, int64_t n, double* x, int64_t inc, double* beta, double* tau) {
+  larfg<double>(alpha, n, x, inc, beta, tau);
+}
+void oracle_dlarf_left(int64_t m, int64_t n, const double* v, int64_t incv, double tau, double* c, int64_t rs,
+                       int64_t cs) {
+  larf_left<double>(m, n, v, incv, tau, c, rs, cs);
+}
+double oracle_dnrm2(int64_t n, const double* x, int64_t inc) { return nrm2<double>(n, x, inc); }
 
 }  // extern "C"

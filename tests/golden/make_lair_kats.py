@@ -28,6 +28,12 @@ SOURCES = {
     "getrs": "src/lapack/getrs.rs",
     "lu": "src/decomposition/lu.rs",
     "iamax": "src/blas/iamax.rs",
+    # QR (the next factorization on the path: geqrf and its reflector helpers)
+    "geqrf": "src/lapack/geqrf.rs",
+    "qr": "src/decomposition/qr.rs",
+    "larfg": "src/lapack/larfg.rs",
+    "larf": "src/lapack/larf.rs",
+    "nrm2": "src/blas/nrm2.rs",
 }
 
 _NUM = r"-?\d[\d_]*(?:\.[\d_]*)?(?:e-?\d+)?(?:_f64|_f32)?"
@@ -119,10 +125,18 @@ def _extract(body: str):
         scalar.append({"macro": m.group(1), "var": m.group(2), "i": int(m.group(3)), "value": _num(m.group(4))})
     for m in re.finditer(r"assert_eq!\((idx|max), (" + _NUM + r")\)", body):
         scalar.append({"macro": "eq", "var": m.group(1), "i": None, "value": _num(m.group(2))})
+    # scalar results compared whole: assert_eq!(beta, 2.), assert_abs_diff_eq!(tau, 1.2, ..)
+    for m in re.finditer(r"assert_(eq|relative_eq|abs_diff_eq)!\(\s*(\w+),\s*(" + _NUM + r")\s*[,)]", body):
+        if m.group(2) not in ("idx", "max"):
+            scalar.append({"macro": m.group(1), "var": m.group(2), "i": None, "value": _num(m.group(3))})
+    # literal arguments of the call under test, e.g. larfg(1., x) or left(&v, 2., &mut c)
+    call_args = [[_num(t) for t in re.findall(r"(?<![\w.])" + _NUM, m.group(2))]
+                 for m in re.finditer(r"super::(larfg|left|right)\(([^;]*)\);", body)]
     shapes = [[int(m.group(2)), int(m.group(3))]
               for m in re.finditer(r"assert_eq!\((\w+)\.shape\(\), &\[(\d+), (\d+)\]\)", body)]
     return {
         "arrays": arrays, "vecs": vecs, "somes": somes, "epsilon": eps, "max_relative": rels,
+        "call_args": call_args,
         "transforms": transforms, "indexed": indexed, "scalar": scalar, "shapes": shapes,
         "singular_none": "singular.is_none()" in body, "empty_pivots": "Vec::<usize>::new()" in body,
     }
