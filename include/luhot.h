@@ -267,6 +267,24 @@ int luhot_factor_read(luhot_factor* f, void* a, int64_t rs, int64_t cs);
 int luhot_factor_device(const luhot_factor* f, const void** d_lu, int64_t* lda, const int32_t** d_piv);
 void luhot_factor_destroy(luhot_factor* f);
 
+/* ---- Householder QR ----------------------------------------------------
+ * Replaces lair's lapack::geqrf (src/lapack/geqrf.rs:9-27), reached through
+ * qr::Factorized::from (src/decomposition/qr.rs:75-86): a (m x n, element
+ * strides) is overwritten by R on and above the diagonal and the reflectors
+ * below it; tau receives min(m, n) scalars.  LUHOT_MODE_EXACT reproduces
+ * lair's arithmetic (larfg's sequential nrm2, larf's increasing-row dots,
+ * separately rounded products and sums) bit for bit. */
+int luhot_dgeqrf(luhot_ctx* ctx, int64_t m, int64_t n, double* a, int64_t rs, int64_t cs, double* tau, int mode);
+int luhot_sgeqrf(luhot_ctx* ctx, int64_t m, int64_t n, float* a, int64_t rs, int64_t cs, float* tau, int mode);
+/* Same on a row-major device matrix (leading dimension lda) and device tau. */
+int luhot_dgeqrf_dev(luhot_ctx* ctx, int64_t m, int64_t n, double* d_a, int64_t lda, double* d_tau, int mode);
+/* Q (m x m, written with element strides q_rs, q_cs) from a factored array
+ * and tau: lair's qr::Factorized::q (src/decomposition/qr.rs:26-60). */
+int luhot_dqr_q(luhot_ctx* ctx, int64_t m, int64_t n, const double* qr, int64_t rs, int64_t cs, const double* tau,
+                double* q, int64_t q_rs, int64_t q_cs, int mode);
+int luhot_sqr_q(luhot_ctx* ctx, int64_t m, int64_t n, const float* qr, int64_t rs, int64_t cs, const float* tau,
+                float* q, int64_t q_rs, int64_t q_cs, int mode);
+
 /* Scratch held by luhot_dgetrs_dev_noalloc in a static device array. */
 #define LUHOT_NOALLOC_SCRATCH_BYTES (4u << 20)
 

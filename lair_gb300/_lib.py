@@ -83,6 +83,11 @@ SIGNATURES = {
     "luhot_factor_read": (_i32, [_vp, _vp, _i64, _i64]),
     "luhot_factor_device": (_i32, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_i64), ctypes.POINTER(_vp)]),
     "luhot_factor_destroy": (None, [_vp]),
+    "luhot_dgeqrf": (_i32, [_vp, _i64, _i64, _vp, _i64, _i64, _vp, _i32]),
+    "luhot_sgeqrf": (_i32, [_vp, _i64, _i64, _vp, _i64, _i64, _vp, _i32]),
+    "luhot_dgeqrf_dev": (_i32, [_vp, _i64, _i64, _vp, _i64, _vp, _i32]),
+    "luhot_dqr_q": (_i32, [_vp, _i64, _i64, _vp, _i64, _i64, _vp, _vp, _i64, _i64, _i32]),
+    "luhot_sqr_q": (_i32, [_vp, _i64, _i64, _vp, _i64, _i64, _vp, _vp, _i64, _i64, _i32]),
     "luhot_dgetrs_dev_noalloc": (_i32, [_i64, _i64, _vp, _i64, _vp, _vp, _i64, _i32, _i32, _vp]),
 }
 
