@@ -319,7 +319,7 @@ def run_ours(args):
         dt = float(tt.item())
         e2e = {"value": world * args.steps * flops_of(n, nrhs) / dt / 1e9, "unit": "GFLOP/s",
                "h2d_bytes_per_step": int(A_h.nbytes + B_h.nbytes), "d2h_bytes_per_step": int(X_h.nbytes),
-               "api": "luhot_dgesv (host A, B in; host X out; pageable numpy buffers)",
+               "api": "luhot_dgesv (host A, B in; host X out; pageable numpy buffers, page-locked by the call)",
                "ms_per_step": dt / args.steps * 1e3}
         _lib.check(lib.luhot_set_stream(ctx, ctypes.c_void_p(stream.cuda_stream)), ctx)
 

@@ -244,6 +244,30 @@ template int stage_out<double>(luhot_ctx*, const double*, int64_t, double*, int6
 template int stage_out<float>(luhot_ctx*, const float*, int64_t, float*, int64_t, int64_t, int64_t, int64_t, DevBuf&);
 template int launch_transpose<double>(luhot_ctx*, const double*, int64_t, double*, int64_t, int, int);
 
+HostPin::HostPin(luhot_ctx* c, const void* base, int64_t m, int64_t n, int64_t rs, int64_t cs, size_t elem)
+    : ctx(c) {
+  if (!base || m <= 0 || n <= 0 || rs < 0 || cs < 0) return;
+  const size_t span = ((size_t)(m - 1) * (size_t)rs + (size_t)(n - 1) * (size_t)cs + 1) * elem;
+  if (span < (size_t)8 << 20) return;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, base) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  if (at.type != cudaMemoryTypeUnregistered) return;
+  if (cudaHostRegister(const_cast<void*>(base), span, cudaHostRegisterDefault) == cudaSuccess)
+    p = const_cast<void*>(base);
+  else
+    cudaGetLastError();
+}
+
+HostPin::~HostPin() {
+  if (!p) return;
+  cudaStreamSynchronize(ctx->stream);
+  cudaHostUnregister(p);
+  cudaGetLastError();
+}
+
 static bool dims_ok(int64_t m, int64_t n) {
   return m >= 0 && n >= 0 && m < (int64_t)INT32_MAX && n < (int64_t)INT32_MAX &&
          (m == 0 || n == 0 || m * n / n == m);
@@ -271,6 +295,7 @@ static int getrf_host(luhot_ctx* ctx, int64_t m, int64_t n, T* a, int64_t rs, in
   if (mode == LUHOT_MODE_EXACT && getrf_uses_colmajor(m, n, rs, cs))
     return getrf_colmajor_host<T>(ctx, m, n, a, rs, cs, piv, singular);
   const int64_t lda = dev_ld<T>(n);
+  HostPin pin_a(ctx, a, m, n, rs, cs, sizeof(T));
   int rc = ensure_buf(ctx, ctx->work[0], (size_t)m * lda * sizeof(T));
   if (rc) return rc;
   rc = ensure_buf(ctx, ctx->piv_buf, (size_t)k * sizeof(int));
@@ -305,6 +330,7 @@ static int getrs_host(luhot_ctx* ctx, int64_t n, int64_t nrhs, const T* lu, int6
       return set_error(ctx, LUHOT_ERR_INVALID_ARG, "getrs: pivot index out of range");
   const int64_t lda = dev_ld<T>(n);
   const int64_t ldb = nrhs;
+  HostPin pin_lu(ctx, lu, n, n, lu_rs, lu_cs, sizeof(T));
   int rc = ensure_buf(ctx, ctx->work[0], (size_t)n * lda * sizeof(T));
   if (rc) return rc;
   rc = ensure_buf(ctx, ctx->work[2], (size_t)n * ldb * sizeof(T));
@@ -482,6 +508,9 @@ int luhot_dgesv(luhot_ctx* ctx, int64_t n, int64_t nrhs, const double* a, int64_
   if (n == 0 || nrhs == 0) return LUHOT_OK;
   if (!a || !b || !x) return set_error(ctx, LUHOT_ERR_INVALID_ARG, "gesv: null pointer");
   const int64_t lda = dev_ld<double>(n);
+  HostPin pin_a(ctx, a, n, n, rs, cs, sizeof(double));
+  HostPin pin_b(ctx, b, n, nrhs, b_rs, b_cs, sizeof(double));
+  HostPin pin_x(ctx, x, n, nrhs, x_rs, x_cs, sizeof(double));
   int rc = ensure_buf(ctx, ctx->work[0], (size_t)n * lda * sizeof(double));
   if (rc) return rc;
   rc = ensure_buf(ctx, ctx->work[2], (size_t)n * nrhs * sizeof(double));

@@ -90,6 +90,7 @@ int factor_create(luhot_ctx* ctx, int64_t m, int64_t n, const T* a, int64_t rs, 
   }
   T* lu = static_cast<T*>(f->d_lu);
   if (k > 0) {
+    HostPin pin_a(ctx, d_a ? nullptr : a, m, n, rs, cs, sizeof(T));
     if (d_a) {
       rc = copy_2d(ctx, lu, f->lda * sizeof(T), d_a, ld_in * sizeof(T), n * sizeof(T), m, cudaMemcpyDeviceToDevice);
     } else {

@@ -16,9 +16,10 @@
 // Exact mode follows lair's arithmetic: nrm2's sequential sum of squares,
 // the dot of each column of C with v summed in increasing row order, every
 // product and sum rounded apart (results are bit-identical to lair).  Fast
-// mode sums in trees and uses FMA.  On GB300 the FP64 pipe (~1.1 TFLOP/s)
-// and HBM (~6.8 TB/s) put this level-2 algorithm (4/3 n^3 flops over ~8 n^3
-// bytes) at the ridge point, so blocking it would not buy much here.
+// mode sums in trees and uses FMA.  This level-2 form reads the trailing
+// block twice and writes it once per column (~24 bytes per element); a
+// blocked (compact-WY) form would move the two updates onto the FP64 tensor
+// pipe.
 #include <algorithm>
 #include <cmath>
 #include <string>
@@ -417,6 +418,7 @@ int geqrf_host(luhot_ctx* ctx, int64_t m, int64_t n, T* a, int64_t rs, int64_t c
   if (k == 0) return LUHOT_OK;
   if (!a || !tau) return set_error(ctx, LUHOT_ERR_INVALID_ARG, "geqrf: null pointer");
   const int64_t lda = qr_ld<T>(n);
+  HostPin pin_a(ctx, a, m, n, rs, cs, sizeof(T));
   int rc = ensure_buf(ctx, ctx->work[0], (size_t)m * lda * sizeof(T) + (size_t)k * sizeof(T) + 256);
   if (rc) return rc;
   T* d_a = static_cast<T*>(ctx->work[0].ptr);

@@ -140,6 +140,19 @@ int getrs_apply(luhot_ctx* ctx, int n, int nrhs, const T* lu, int64_t lda, const
 template <typename T, typename TA = T>
 int invert_diag_blocks(luhot_ctx* ctx, int n, const TA* lu, int64_t lda, T* dinv_l, T* dinv_u);
 
+// Page-locks a caller's host array for the duration of one call (large
+// arrays only, if not already registered), so its copies run as DMA at the
+// host link's full rate whatever the state of the pageable memory; the stream
+// is synchronised before the pages are released.  Strides in elements.
+struct HostPin {
+  HostPin(luhot_ctx* ctx, const void* base, int64_t m, int64_t n, int64_t rs, int64_t cs, size_t elem);
+  ~HostPin();
+  HostPin(const HostPin&) = delete;
+  HostPin& operator=(const HostPin&) = delete;
+  luhot_ctx* ctx = nullptr;
+  void* p = nullptr;
+};
+
 // Held by every C entry point: serialises calls on a context, makes its
 // device current and clears the last error message.
 struct CtxGuard {
