@@ -12,8 +12,9 @@
 //                     pivot keys, warp-shuffle reduce, deterministic order),
 //                     row interchanges as id swaps, and the update of the
 //                     previous step overlapping the exchange.
-//   2. laswp_kernel   applies the w interchanges to the columns left and
-//                     right of the panel (coalesced 16-byte row moves).
+//   2. laswp_moves_kernel  applies the panel's interchanges to the columns
+//                     left and right of it, as a gather of the (at most 2w)
+//                     rows that moved.
 //   3. trsm_kernel    U12 <- L11^-1 A12 (unit lower).
 //   4. gemm_*_kernel  A22 <- A22 - L21 U12 (the Schur complement).
 //
@@ -64,6 +65,8 @@ struct PanelArgs {
   int lds;        // shared-memory row stride (elements)
   int* piv;       // device pivots (global row index per step)
   unsigned long long* slots;  // [2][kMaxPanelCtas][kPanelSlotWords] exchange words
+  int* moves;                 // (destination, source) rows of the panel's rows that moved
+  int* move_count;            // zeroed before the launch
   DeviceStatus* st;
 };
 
@@ -286,6 +289,7 @@ __global__ void __launch_bounds__(256) panel_kernel(PanelArgs<T> p) {
   T* S = reinterpret_cast<T*>(smem_raw);                        // [rows_per][lds]
   T* segb = S + (size_t)p.rows_per * p.lds;                     // [2][kMaxPanelWidth] pivot rows
   int* ids = reinterpret_cast<int*>(segb + 2 * kMaxPanelWidth);  // [rows_per] global row of each slot
+  int* orig = ids + p.rows_per;  // [rows_per] the row each slot's content started in
   __shared__ K red_k[8];
   __shared__ int red_i[8], red_s[8];
   __shared__ int s_ok, s_r0, s_pivoted, s_ret;
@@ -308,7 +312,7 @@ __global__ void __launch_bounds__(256) panel_kernel(PanelArgs<T> p) {
     const int r = idx / w, c = idx - r * w;
     S[r * lds + c] = p.a[(int64_t)(r_begin + r) * p.lda + p.k0 + c];
   }
-  for (int r = tid; r < nloc; r += blockDim.x) ids[r] = r_begin + r;
+  for (int r = tid; r < nloc; r += blockDim.x) ids[r] = orig[r] = r_begin + r;
   if (tid == 0) s_r0 = 0;
   __syncthreads();
   {
@@ -466,6 +470,9 @@ __global__ void __launch_bounds__(256) panel_kernel(PanelArgs<T> p) {
           const int t = ids[ret];
           ids[ret] = ids[r0];
           ids[r0] = t;
+          const int o = orig[ret];
+          orig[ret] = orig[r0];
+          orig[r0] = o;
         }
       }
       ++r0;
@@ -507,33 +514,44 @@ __global__ void __launch_bounds__(256) panel_kernel(PanelArgs<T> p) {
     const int r = idx / w, c = idx - r * w;
     p.a[(int64_t)ids[r] * p.lda + p.k0 + c] = S[r * lds + c];
   }
-}
-
-// ---------------------------------------------------------------------------
-// 2. Row interchanges outside the panel.  Each thread owns one column (or a
-//    16-byte pair/quad) and replays the w swaps in order, as
-//    src/lapack/laswp.rs:11-40 does row by row.
-// ---------------------------------------------------------------------------
-template <typename T>
-__global__ void laswp_kernel(T* a, int64_t lda, const int* piv, int k0, int w, int c_left_end,
-                             int c_right_begin, int n) {
-  const int nleft = c_left_end;
-  const int nright = max(0, n - c_right_begin);
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nleft + nright) return;
-  const int c = (t < nleft) ? t : (c_right_begin + t - nleft);
-  for (int s = 0; s < w; ++s) {
-    const int i = k0 + s;
-    const int pr = piv[i];
-    if (pr != i) {
-      T* x = a + (int64_t)i * lda + c;
-      T* y = a + (int64_t)pr * lda + c;
-      const T tmp = *x;
-      *x = *y;
-      *y = tmp;
+  // The rows that changed place, for the interchanges outside the panel.
+  for (int r = tid; r < nloc; r += blockDim.x) {
+    if (ids[r] != orig[r]) {
+      const int e = atomicAdd(p.move_count, 1);
+      if (e < 2 * kMaxPanelWidth) {  // at most 2w rows move; the bound guards the list
+        p.moves[2 * e] = ids[r];
+        p.moves[2 * e + 1] = orig[r];
+      }
     }
   }
 }
+
+// ---------------------------------------------------------------------------
+// 2. Row interchanges outside the panel, from the panel's list of moved rows
+//    (the composition of its w interchanges: at most 2w rows, each row's
+//    final content comes from one source row).  A CTA takes 32 columns: it
+//    loads every moved row's source values into shared memory, then stores
+//    them at the destinations -- all loads independent, 256-byte row
+//    segments.  Pure data movement, so exact mode is unaffected.
+template <typename T>
+__global__ void __launch_bounds__(256) laswp_moves_kernel(T* a, int64_t lda, const int* moves,
+                                                          const int* move_count, int capacity, int c_left_end,
+                                                          int c_right_begin, int n) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* vals = reinterpret_cast<T*>(smem_raw);  // [capacity][32]
+  const int count = min(*move_count, capacity);
+  const int nleft = c_left_end;
+  const int t = blockIdx.x * 32 + threadIdx.x;
+  const int nright = max(0, n - c_right_begin);
+  const bool on = t < nleft + nright;
+  const int c = (t < nleft) ? t : (c_right_begin + t - nleft);
+  for (int e = threadIdx.y; e < count; e += blockDim.y)
+    if (on) vals[e * 32 + threadIdx.x] = a[(int64_t)moves[2 * e + 1] * lda + c];
+  __syncthreads();
+  for (int e = threadIdx.y; e < count; e += blockDim.y)
+    if (on) a[(int64_t)moves[2 * e] * lda + c] = vals[e * 32 + threadIdx.x];
+}
+
 
 // ---------------------------------------------------------------------------
 // 3. U12 <- L11^-1 A12 for rows [k0, k0+w), columns [c0, n).  One thread per
@@ -892,7 +910,7 @@ __global__ void __launch_bounds__(256, 1) gemm_dmma_persistent_kernel(double* a,
 // ---------------------------------------------------------------------------
 template <typename T>
 static size_t panel_smem_bytes(int rows_per, int w) {
-  return ((size_t)rows_per * (w + 1) + 2 * kMaxPanelWidth) * sizeof(T) + (size_t)rows_per * sizeof(int);
+  return ((size_t)rows_per * (w + 1) + 2 * kMaxPanelWidth) * sizeof(T) + 2 * (size_t)rows_per * sizeof(int);
 }
 
 template <typename T, bool kExact>
@@ -932,7 +950,10 @@ static int launch_panel(luhot_ctx* ctx, T* a, int64_t lda, int m, int k0, int w,
   args.lds = w + 1;
   args.piv = piv;
   args.slots = static_cast<unsigned long long*>(ctx->panel_scratch);
+  args.moves = reinterpret_cast<int*>(static_cast<char*>(ctx->panel_scratch) + kPanelSlotBytes);
+  args.move_count = args.moves + 4 * kMaxPanelWidth;
   args.st = ctx->d_status;
+  LUHOT_CUDA_TRY(ctx, cudaMemsetAsync(args.move_count, 0, sizeof(int), stream));
   void* kargs[] = {&args};
   prof_begin(ctx, kProfPanel);
   LUHOT_CUDA_TRY(ctx, cudaLaunchCooperativeKernel((void*)kern, dim3(P), dim3(256), kargs, smem,
@@ -996,8 +1017,12 @@ static int getrf_impl(luhot_ctx* ctx, int m, int n, T* a, int64_t lda, int* piv,
     const int ncols_swap = k0 + std::max(0, n - c_right);
     if (ncols_swap > 0) {
       prof_begin(ctx, kProfLaswp);
-      laswp_kernel<T><<<(ncols_swap + 255) / 256, 256, 0, stream>>>(a, lda, piv, k0, w, k0, c_right,
-                                                                    n);
+      int* moves = reinterpret_cast<int*>(static_cast<char*>(ctx->panel_scratch) + kPanelSlotBytes);
+      const size_t lsm = (size_t)2 * w * 32 * sizeof(T);
+      LUHOT_CUDA_TRY(ctx, cudaFuncSetAttribute(laswp_moves_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)lsm));
+      laswp_moves_kernel<T><<<(ncols_swap + 31) / 32, dim3(32, 8), lsm, stream>>>(
+          a, lda, moves, moves + 4 * kMaxPanelWidth, 2 * w, k0, c_right, n);
       prof_end(ctx, kProfLaswp, 0.0, 4.0 * w * ncols_swap * sizeof(T));
       LUHOT_CUDA_TRY(ctx, cudaGetLastError());
     }

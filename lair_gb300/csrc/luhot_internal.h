@@ -24,7 +24,11 @@ constexpr int kMaxPanelWidth = 128;    // sizes the panel kernel's scratch
 // (payload, step tag), two words per FP64 value.
 constexpr int kPanelHeaderWords = 6;
 constexpr int kPanelSlotWords = kPanelHeaderWords + 2 * kMaxPanelWidth;
-constexpr size_t kPanelScratchBytes = 2 * (size_t)kMaxPanelCtas * kPanelSlotWords * sizeof(unsigned long long);
+constexpr size_t kPanelSlotBytes = 2 * (size_t)kMaxPanelCtas * kPanelSlotWords * sizeof(unsigned long long);
+// Followed by the panel's row moves: up to 2 * kMaxPanelWidth (destination,
+// source) pairs and their count.
+constexpr size_t kPanelMovesBytes = (4 * (size_t)kMaxPanelWidth + 64) * sizeof(int);
+constexpr size_t kPanelScratchBytes = kPanelSlotBytes + kPanelMovesBytes;
 
 // Grow-only device buffer.
 struct DevBuf {
