@@ -357,11 +357,10 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
-def conditioned_system(n, kappa, seed, torch):
-    """A = Q1 diag(sigma) Q2^T, Q from Householder QR of seeded N(0,1) matrices
-    (FP32 QR on the GPU: the orthogonality error ~1e-6 perturbs the singular
-    values only relatively, so kappa is kept), sigma geometric 1 -> 1/kappa,
-    product formed in FP64; b iid N(0,1)."""
+def orthogonal_factors(n, seed, torch):
+    """Q1, Q2 from Householder QR of seeded N(0,1) matrices (FP32 QR on the
+    GPU: the orthogonality error ~1e-6 perturbs the singular values only
+    relatively, so kappa is kept) and b iid N(0,1)."""
     gen = torch.Generator(device="cuda").manual_seed(seed)
     g1 = torch.randn((n, n), device="cuda", generator=gen)
     g2 = torch.randn((n, n), device="cuda", generator=gen)
@@ -375,11 +374,15 @@ def conditioned_system(n, kappa, seed, torch):
         q1 = torch.from_numpy(np.linalg.qr(g1.cpu().numpy())[0]).cuda()
         q2 = torch.from_numpy(np.linalg.qr(g2.cpu().numpy())[0]).cuda()
     del g1, g2
-    sigma = torch.logspace(0, -float(np.log10(kappa)), n, dtype=torch.float64, device="cuda")
-    a = (q1.double() * sigma) @ q2.double().T
-    del q1, q2
     b = torch.randn(n, dtype=torch.float64, device="cuda", generator=gen)
-    return a.contiguous(), b
+    return q1, q2, b
+
+
+def conditioned_matrix(q1, q2, kappa, torch):
+    """A = Q1 diag(sigma) Q2^T, sigma geometric 1 -> 1/kappa, formed in FP64."""
+    n = q1.shape[0]
+    sigma = torch.logspace(0, -float(np.log10(kappa)), n, dtype=torch.float64, device="cuda")
+    return ((q1.double() * sigma) @ q2.double().T).contiguous()
 
 
 def run_ir(args, lib, ctx, torch, rank):
@@ -392,14 +395,14 @@ def run_ir(args, lib, ctx, torch, rank):
     n = args.ir_n
     kappa = args.ir_kappa
     t0 = time.perf_counter()
-    A, b = conditioned_system(n, kappa, 7 + rank, torch)
+    q1, q2, b = orthogonal_factors(n, 7 + rank, torch)
+    A = conditioned_matrix(q1, q2, kappa, torch)
     torch.cuda.synchronize()
     gen_s = time.perf_counter() - t0
     x = torch.empty_like(b)
     stream = torch.cuda.current_stream()
-    results = {}
-    for prec, solver in (("fp32", "ir"), ("bf16x3", "ir"), ("bf16x3", "gmres"), ("fp32", "gmres"), ("tf32", "gmres"),
-                         ("fp16", "gmres"), ("bf16", "gmres")):
+
+    def measure(A, prec, solver, reps, warmup):
         info = _lib.IrInfo()
         status = {"rc": 0}
 
@@ -410,9 +413,7 @@ def run_ir(args, lib, ctx, torch, rank):
             if status["rc"] not in (0, _lib.LUHOT_ERR_NOT_CONVERGED):
                 _lib.check(status["rc"], ctx)
 
-        headline = solver == "ir"
-        reps = args.steps if headline else 1
-        for _ in range(args.warmup if headline else 1):
+        for _ in range(warmup):
             solve()
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -424,10 +425,31 @@ def run_ir(args, lib, ctx, torch, rank):
         ms = e0.elapsed_time(e1) / reps
         R = b - A @ x
         berr = (R.abs().max() / (A.abs().sum(1).max() * x.abs().max() + b.abs().max())).item()
-        results[f"{prec}/{solver}"] = {
-            "ms": ms, "gflops": flops_of(n, 1) / (ms * 1e-3) / 1e9, "iterations": info.iterations,
-            "inner_iterations": info.inner_iterations, "backward_error": berr, "converged": status["rc"] == 0,
-            "berr_ok": berr <= n * EPS64, "factor_ms": info.factor_ms, "refine_ms": info.refine_ms}
+        return {"ms": ms, "gflops": flops_of(n, 1) / (ms * 1e-3) / 1e9, "iterations": info.iterations,
+                "inner_iterations": info.inner_iterations, "backward_error": berr, "converged": status["rc"] == 0,
+                "berr_ok": berr <= n * EPS64, "factor_ms": info.factor_ms, "refine_ms": info.refine_ms}
+
+    results = {}
+    for prec, solver in (("fp32", "ir"), ("bf16x3", "ir"), ("bf16x3", "gmres"), ("fp32", "gmres"), ("tf32", "gmres"),
+                         ("fp16", "gmres"), ("bf16", "gmres")):
+        headline = solver == "ir"
+        results[f"{prec}/{solver}"] = measure(A, prec, solver, args.steps if headline else 1,
+                                              args.warmup if headline else 1)
+    # the other condition numbers of the workload: same Q1, Q2 and b, one timed solve each
+    sweep = {}
+    if not args.no_ir_sweep:
+        for kap in (1e2, 1e4):
+            Ak = conditioned_matrix(q1, q2, kap, torch)
+            runs = {}
+            for prec, solver in (("bf16x3", "ir"), ("fp32", "ir"), ("tf32", "ir"), ("fp16", "ir"), ("bf16", "gmres"),
+                                 ("tf32", "gmres")):
+                r = measure(Ak, prec, solver, 1, 1)
+                runs[f"{prec}/{solver}"] = {k: r[k] for k in ("ms", "iterations", "inner_iterations",
+                                                              "backward_error", "converged", "factor_ms")}
+            ok = [k for k in runs if runs[k]["converged"] and runs[k]["backward_error"] <= n * EPS64]
+            sweep[f"{kap:g}"] = {"runs": runs, "best": min(ok, key=lambda k: runs[k]["ms"]) if ok else None}
+            del Ak
+    del q1, q2
     # plain FP64 LU on the same system, once
     Aw = A.clone()
     piv = torch.empty(n, dtype=torch.int32, device="cuda")
@@ -450,7 +472,8 @@ def run_ir(args, lib, ctx, torch, rank):
             "n": n, "kappa": kappa, "generation_s": gen_s, "runs": results,
             "fp64_lu_ms": fp64_ms, "fp64_lu_gflops": flops_of(n, 1) / (fp64_ms * 1e-3) / 1e9,
             "fp64_backward_error": fp64_berr, "best": best, "best_gflops": results[best]["gflops"],
-            "speedup_vs_fp64": fp64_ms / results[best]["ms"], "berr_bound": n * EPS64}
+            "speedup_vs_fp64": fp64_ms / results[best]["ms"], "berr_bound": n * EPS64,
+            "kappa_sweep": sweep}
 
 
 def run_qr(args, lib, ctx, torch):
@@ -594,6 +617,8 @@ def main():
     ap.add_argument("--batch-loop-sample", type=int, default=300)
     ap.add_argument("--ir-n", type=int, default=16384)
     ap.add_argument("--ir-kappa", type=float, default=1e6)
+    ap.add_argument("--no-ir-sweep", action="store_true",
+                    help="skip the kappa = 1e2 and 1e4 runs of the refinement leg")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

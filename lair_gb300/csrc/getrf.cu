@@ -9,9 +9,10 @@
 //   1. panel_kernel   cooperative; factors rows [k0, m) x cols [k0, k0+w) held
 //                     in shared memory across all CTAs; per column one
 //                     exchange of step-tagged candidates through L2 (integer
-//                     pivot keys, warp-shuffle reduce, deterministic order),
-//                     row interchanges as id swaps, and the update of the
-//                     previous step overlapping the exchange.
+//                     pivot keys, redux.sync reduce, deterministic order; the
+//                     winner's row segment follows by cp.async off the
+//                     critical path), row interchanges as id swaps, and the
+//                     update of the previous step overlapping the exchange.
 //   2. laswp_moves_kernel  applies the panel's interchanges to the columns
 //                     left and right of it, as a gather of the (at most 2w)
 //                     rows that moved.
@@ -89,6 +90,7 @@ struct PivotKey<float> {
   }
   __device__ static K shfl_xor(K k, int off) { return __shfl_xor_sync(0xffffffffu, k, off); }
   __device__ static K shfl(K k, int src) { return __shfl_sync(0xffffffffu, k, src); }
+  __device__ static float value(K raw) { return __uint_as_float(raw); }
 };
 template <>
 struct PivotKey<double> {
@@ -99,6 +101,7 @@ struct PivotKey<double> {
   }
   __device__ static K shfl_xor(K k, int off) { return __shfl_xor_sync(0xffffffffu, k, off); }
   __device__ static K shfl(K k, int src) { return __shfl_sync(0xffffffffu, k, src); }
+  __device__ static double value(K raw) { return __longlong_as_double((long long)raw); }
 };
 
 template <typename K>
@@ -109,11 +112,30 @@ __device__ __forceinline__ void key_combine(K& k, int& i, int& s, K k2, int i2, 
     s = s2;
   }
 }
-template <typename T>
-__device__ __forceinline__ void key_reduce_warp(typename PivotKey<T>::K& k, int& i, int& s, int width) {
-  for (int off = width >> 1; off > 0; off >>= 1)
-    key_combine(k, i, s, PivotKey<T>::shfl_xor(k, off), __shfl_xor_sync(0xffffffffu, i, off),
-                __shfl_xor_sync(0xffffffffu, s, off));
+// Warp-wide reduction of (key, id, slot) on the integer reduce unit
+// (redux.sync): the largest key, then the smallest id among the lanes that
+// hold it; the slot comes from that lane, whose index is returned.  The
+// order is total, so this is the answer of any key_combine tree.
+__device__ __forceinline__ int key_reduce_redux(unsigned int& k, int& i, int& s) {
+  const unsigned int m = __reduce_max_sync(0xffffffffu, k);
+  const int mi = __reduce_min_sync(0xffffffffu, k == m ? i : INT_MAX);
+  const int src = __ffs(__ballot_sync(0xffffffffu, k == m && i == mi)) - 1;
+  s = __shfl_sync(0xffffffffu, s, src);
+  k = m;
+  i = mi;
+  return src;
+}
+__device__ __forceinline__ int key_reduce_redux(unsigned long long& k, int& i, int& s) {
+  const unsigned int hi = (unsigned int)(k >> 32);
+  const unsigned int mh = __reduce_max_sync(0xffffffffu, hi);
+  const unsigned int ml = __reduce_max_sync(0xffffffffu, hi == mh ? (unsigned int)k : 0u);
+  const unsigned long long m = ((unsigned long long)mh << 32) | ml;
+  const int mi = __reduce_min_sync(0xffffffffu, k == m ? i : INT_MAX);
+  const int src = __ffs(__ballot_sync(0xffffffffu, k == m && i == mi)) - 1;
+  s = __shfl_sync(0xffffffffu, s, src);
+  k = m;
+  i = mi;
+  return src;
 }
 
 // Exchange words: payload in the low 32 bits, the step tag in the high 32.
@@ -133,45 +155,61 @@ __device__ __forceinline__ void st_word(unsigned long long* p, unsigned int bits
 __device__ __forceinline__ bool word_ok(unsigned long long v, unsigned int tag) {
   return (unsigned int)(v >> 32) == tag;
 }
-// Values and keys as one (FP32) or two (FP64) tagged words.
+// Four words (one 32-byte L2 sector) in one load; each 8-byte element is
+// read whole.  p 32-byte aligned.
+__device__ __forceinline__ void ld_quad(const unsigned long long* p, unsigned long long* v) {
+  asm volatile("ld.relaxed.gpu.global.v4.u64 {%0, %1, %2, %3}, [%4];"
+               : "=l"(v[0]), "=l"(v[1]), "=l"(v[2]), "=l"(v[3])
+               : "l"(p)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+// 16 bytes global -> shared through L2 (cp.async.cg), completed by
+// cp_async_wait_all; no register holds the data in between.
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
+  const unsigned int d = (unsigned int)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(gmem_src) : "memory");
+}
+
+// Values and keys as one (FP32) or two (FP64) tagged words.  The header of
+// a CTA's slot holds its candidate's key with the pivot's sign in the top
+// bit (so the key word also gives the pivot value), the row id, and the
+// candidate's column j+1 value: words [0, 4 * kHdrQuads), whole 32-byte
+// sectors of the slot (slots are 32-byte aligned).
 template <typename T>
 struct Tagged;
 template <>
 struct Tagged<float> {
+  using K = unsigned int;
   static constexpr int kWords = 1;
+  static constexpr int kIdW = 1, kU1W = 2, kHdrQuads = 1;
+  static constexpr K kSign = 0x80000000u;
   __device__ static void put(unsigned long long* p, float v, unsigned int tag) { st_word(p, __float_as_uint(v), tag); }
-  __device__ static bool get(const unsigned long long* p, unsigned int tag, float& v) {
-    const unsigned long long x = ld_word(p);
-    v = __uint_as_float((unsigned int)x);
-    return word_ok(x, tag);
-  }
-  __device__ static void put_key(unsigned long long* p, unsigned int k, unsigned int tag) { st_word(p, k, tag); }
-  __device__ static bool get_key(const unsigned long long* p, unsigned int tag, unsigned int& k) {
-    const unsigned long long x = ld_word(p);
-    k = (unsigned int)x;
-    return word_ok(x, tag);
-  }
+  __device__ static void put_key(unsigned long long* p, K k, unsigned int tag) { st_word(p, k, tag); }
+  __device__ static K bits(const unsigned long long* w) { return (unsigned int)w[0]; }
+  __device__ static float value(const unsigned long long* w) { return __uint_as_float((unsigned int)w[0]); }
+  __device__ static bool ok(const unsigned long long* w, unsigned int tag) { return word_ok(w[0], tag); }
 };
 template <>
 struct Tagged<double> {
+  using K = unsigned long long;
   static constexpr int kWords = 2;
-  __device__ static void put(unsigned long long* p, double v, unsigned int tag) {
-    put_key(p, (unsigned long long)__double_as_longlong(v), tag);
-  }
-  __device__ static bool get(const unsigned long long* p, unsigned int tag, double& v) {
-    unsigned long long b;
-    const bool ok = get_key(p, tag, b);
-    v = __longlong_as_double((long long)b);
-    return ok;
-  }
-  __device__ static void put_key(unsigned long long* p, unsigned long long k, unsigned int tag) {
+  static constexpr int kIdW = 2, kU1W = 3, kHdrQuads = 2;
+  static constexpr K kSign = 0x8000000000000000ull;
+  __device__ static void put_key(unsigned long long* p, K k, unsigned int tag) {
     st_word(p, (unsigned int)(k >> 32), tag);
     st_word(p + 1, (unsigned int)k, tag);
   }
-  __device__ static bool get_key(const unsigned long long* p, unsigned int tag, unsigned long long& k) {
-    const unsigned long long hi = ld_word(p), lo = ld_word(p + 1);
-    k = ((unsigned long long)(unsigned int)hi << 32) | (unsigned int)lo;
-    return word_ok(hi, tag) && word_ok(lo, tag);
+  __device__ static void put(unsigned long long* p, double v, unsigned int tag) {
+    put_key(p, (unsigned long long)__double_as_longlong(v), tag);
+  }
+  __device__ static K bits(const unsigned long long* w) {
+    return ((unsigned long long)(unsigned int)w[0] << 32) | (unsigned int)w[1];
+  }
+  __device__ static double value(const unsigned long long* w) { return __longlong_as_double((long long)bits(w)); }
+  __device__ static bool ok(const unsigned long long* w, unsigned int tag) {
+    return word_ok(w[0], tag) && word_ok(w[1], tag);
   }
 };
 
@@ -188,11 +226,51 @@ __device__ __forceinline__ bool panel_wait_over(DeviceStatus* st, unsigned long 
   return __shfl_sync(0xffffffffu, late, 0) != 0 || __any_sync(0xffffffffu, ld_relaxed_i32(&st->abort) != 0);
 }
 
+// FP32 rows in 16-byte chunks: lane (sub, ch) of a warp takes columns
+// [4ch, 4ch+4) of row sub of the warp's current row group (W/4 chunks a row,
+// 32/(W/4) rows a warp instruction); two row groups per pass with all loads
+// first.  Columns left of c0 in the first chunk keep their value (the same
+// single update per element as the scalar form, so exact mode is unchanged);
+// chunks at or beyond the padded width are not touched.  Needs rows and u
+// 16-byte aligned (lds and the row base multiples of 4 floats).
+template <int W, bool kExact>
+__device__ __forceinline__ void panel_update_f32x4(float* S, int lds, int r0, int nloc, int skip, int jj, int c0,
+                                                   int w, const float* u, int t, int nt) {
+  constexpr int CH = W / 4, RPW = 32 / CH, kR = 2;
+  const int lane = t & 31, wi = t >> 5, nw = nt >> 5;
+  const int ch = lane % CH, sub = lane / CH;
+  const int c = ch * 4;
+  if (c + 4 <= c0 || c >= w || r0 >= nloc) return;
+  const float4 uv = *reinterpret_cast<const float4*>(u + c);
+  const int G = nw * RPW;
+  for (int rb = r0 + wi * RPW + sub; rb < nloc; rb += kR * G) {
+    float l[kR];
+    float4 x[kR];
+#pragma unroll
+    for (int e = 0; e < kR; ++e) {
+      const float* row = S + (rb + e * G < nloc ? rb + e * G : rb) * lds;
+      l[e] = row[jj];
+      x[e] = *reinterpret_cast<const float4*>(row + c);
+    }
+#pragma unroll
+    for (int e = 0; e < kR; ++e) {
+      const int r = rb + e * G;
+      if (r < nloc && r != skip) {
+        float4 y = x[e];
+        if (c + 0 >= c0) y.x = upd<kExact>(y.x, l[e], uv.x);
+        if (c + 1 >= c0) y.y = upd<kExact>(y.y, l[e], uv.y);
+        if (c + 2 >= c0) y.z = upd<kExact>(y.z, l[e], uv.z);
+        if (c + 3 >= c0) y.w = upd<kExact>(y.w, l[e], uv.w);
+        *reinterpret_cast<float4*>(S + r * lds + c) = y;
+      }
+    }
+  }
+}
 // A[r][c] -= A[r][jj] * u[c] for the rows [r0, nloc) other than `skip` and
 // the columns [c0, w), by threads t of nt (a multiple of 32).  FP64 flattens
 // (row, column) pairs so every lane is busy (the FP64 pipe bounds it); FP32
 // gives each warp whole rows, lanes along the columns (no index arithmetic
-// per element; latency bounds it).
+// per element; shared-memory latency bounds it, hence the batched loads).
 template <typename T, bool kExact>
 __device__ __forceinline__ void panel_update(T* S, int lds, int r0, int nloc, int skip, int jj, int c0, int w,
                                              const T* u, int t, int nt) {
@@ -234,29 +312,10 @@ __device__ __forceinline__ void panel_update(T* S, int lds, int r0, int nloc, in
       if (do_b) S[rb * lds + c0 + cb] = upd<kExact>(xb, lb, ub);
     }
   } else {
-    const int lane = t & 31, wi = t >> 5, nw = nt >> 5;
-    T ur[kMaxPanelWidth / 32];
-#pragma unroll
-    for (int q = 0; q < kMaxPanelWidth / 32; ++q) {
-      const int c = c0 + lane + 32 * q;
-      ur[q] = c < w ? u[c] : T(0);
-    }
-    for (int r = r0 + wi; r < nloc; r += 2 * nw) {
-      const int rb = r + nw;
-      const bool a_on = r != skip, b_on = rb < nloc && rb != skip;
-      T* ra = S + r * lds;
-      T* rbp = S + (b_on ? rb : r) * lds;
-      const T la = ra[jj], lb = rbp[jj];
-#pragma unroll
-      for (int q = 0; q < kMaxPanelWidth / 32; ++q) {
-        const int c = c0 + lane + 32 * q;
-        if (32 * q < wc && c < w) {
-          const T xa = ra[c], xb = rbp[c];
-          if (a_on) ra[c] = upd<kExact>(xa, la, ur[q]);
-          if (b_on) rbp[c] = upd<kExact>(xb, lb, ur[q]);
-        }
-      }
-    }
+    if (w <= 64)
+      panel_update_f32x4<64, kExact>(S, lds, r0, nloc, skip, jj, c0, w, u, t, nt);
+    else
+      panel_update_f32x4<128, kExact>(S, lds, r0, nloc, skip, jj, c0, w, u, t, nt);
   }
 }
 
@@ -270,33 +329,40 @@ __device__ __forceinline__ void panel_update(T* S, int lds, int r0, int nloc, in
 //
 // Per column j (elimination step ul = k0 + j), with the update of step j-1
 // to columns j+1.. still pending for all rows but this CTA's candidate row:
-//   warp 0:     finish the candidate row's pending update; publish its key
-//               (|pivot| bits), row id, segment j.. and 1/pivot as tagged
-//               words; poll the P headers until all carry this step's tag,
-//               folding them into the winner; read the winner's segment and
-//               reciprocal; relabel the ids of rows ul and pr.
+//   warp 0:     publish the candidate's header (key = |pivot| bits with the
+//               pivot's sign on top, row id, column j+1 value after the
+//               pending update), then finish the candidate row's pending
+//               update and publish its segment j+2.., all as tagged words;
+//               poll the P headers until all carry this step's tag, folding
+//               them into the winner (the pivot and its column j+1 value come
+//               with its header); start the copy of the winner's segment into
+//               shared memory (cp.async); relabel the ids of rows ul and pr.
 //   warps 1-7:  meanwhile, the pending update of step j-1 (columns j+1..),
 //               which thus overlaps the exchange.
 //   barrier;    the pivot row's CTA retires it; all warps scale column j,
-//               update column j+1 only and find its candidates; barrier.
+//               update column j+1 only and find its candidates; warp 0 checks
+//               the copied segment's tags and keeps it for the next step's
+//               updates; barrier.
 // The arithmetic and its order per element are those of lair's
 // getrf_row_major (src/lapack/getrf.rs:56-89): 1/p rounded, l = a*(1/p)
 // rounded, a - l*u (separately rounded in exact mode), steps in order.
 template <typename T, bool kExact>
-__global__ void __launch_bounds__(256) panel_kernel(PanelArgs<T> p) {
+__global__ void __launch_bounds__(512, 1) panel_kernel(PanelArgs<T> p) {
   using K = typename PivotKey<T>::K;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* S = reinterpret_cast<T*>(smem_raw);                        // [rows_per][lds]
   T* segb = S + (size_t)p.rows_per * p.lds;                     // [2][kMaxPanelWidth] pivot rows
   int* ids = reinterpret_cast<int*>(segb + 2 * kMaxPanelWidth);  // [rows_per] global row of each slot
   int* orig = ids + p.rows_per;  // [rows_per] the row each slot's content started in
-  __shared__ K red_k[8];
-  __shared__ int red_i[8], red_s[8];
+  __shared__ K red_k[16];
+  __shared__ int red_i[16], red_s[16];
+  __shared__ int ulslot[kMaxPanelWidth];  // slot holding row id k0 + jj in this CTA, or -1
+  __shared__ __align__(16) unsigned long long stage[2 * kMaxPanelWidth];  // the winner's segment words
   __shared__ int s_ok, s_r0, s_pivoted, s_ret;
-  __shared__ T s_recip;
+  __shared__ T s_recip, s_u1;
 
   constexpr unsigned kFull = 0xffffffffu;
-  constexpr int kWarps = 8;
+  const int kWarps = blockDim.x >> 5;  // 8 or 16
   constexpr int kW = Tagged<T>::kWords;
   constexpr int kHdr = kPanelHeaderWords;
   const int P = gridDim.x;
@@ -313,14 +379,21 @@ __global__ void __launch_bounds__(256) panel_kernel(PanelArgs<T> p) {
     S[r * lds + c] = p.a[(int64_t)(r_begin + r) * p.lda + p.k0 + c];
   }
   for (int r = tid; r < nloc; r += blockDim.x) ids[r] = orig[r] = r_begin + r;
-  if (tid == 0) s_r0 = 0;
+  for (int jj = tid; jj < w; jj += blockDim.x) {
+    const int s = p.k0 + jj - r_begin;
+    ulslot[jj] = (s >= 0 && s < nloc) ? s : -1;
+  }
+  if (tid == 0) {
+    s_r0 = 0;
+    s_ok = 1;
+  }
   __syncthreads();
   {
     // Column 0 candidates.
     K bk = 0;
     int bi = INT_MAX, bs = -1;
     for (int r = tid; r < nloc; r += blockDim.x) key_combine(bk, bi, bs, PivotKey<T>::of(S[r * lds]), ids[r], r);
-    key_reduce_warp<T>(bk, bi, bs, 32);
+    key_reduce_redux(bk, bi, bs);
     if (lane == 0) {
       red_k[warp] = bk;
       red_i[warp] = bi;
@@ -337,39 +410,51 @@ __global__ void __launch_bounds__(256) panel_kernel(PanelArgs<T> p) {
     const unsigned int tag = (unsigned int)ul + 1u;
     unsigned long long* slots = p.slots + (size_t)(j & 1) * kMaxPanelCtas * kPanelSlotWords;
     T* seg = segb + (j & 1) * kMaxPanelWidth;
-    // The CTA's candidate for column j (every warp reduces the same eight).
+    // The CTA's candidate for column j (lanes below kWarps hold the warps').
     K ck = lane < kWarps ? red_k[lane] : K(0);
     int ci = lane < kWarps ? red_i[lane] : INT_MAX;
     int cs = lane < kWarps ? red_s[lane] : -1;
-    key_reduce_warp<T>(ck, ci, cs, kWarps);
-    ck = PivotKey<T>::shfl(ck, 0);
-    ci = __shfl_sync(kFull, ci, 0);
-    cs = __shfl_sync(kFull, cs, 0);
+    key_reduce_redux(ck, ci, cs);
+    bool seg_live = false;  // the winner's segment j+2.. is being copied into stage
+    const unsigned long long* wseg = nullptr;
+    unsigned long long t0 = 0;
     if (warp == 0) {
-      if (dj >= 0 && cs >= 0) {
-        // The candidate row's pending update, before it is published.
-        const T* up = segb + (dj & 1) * kMaxPanelWidth;
-        const T l = S[cs * lds + dj];
-        for (int c = dj + 2 + lane; c < w; c += 32) S[cs * lds + c] = upd<kExact>(S[cs * lds + c], l, up[c]);
-        __syncwarp();
-      }
-      // Publish: segment j.., the header, then 1/pivot (its division
-      // overlaps the other CTAs' publishing).
       unsigned long long* mine = slots + (size_t)b * kPanelSlotWords;
-      if (cs >= 0)
-        for (int c = j + lane; c < w; c += 32) Tagged<T>::put(mine + kHdr + c * kW, S[cs * lds + c], tag);
+      const T* up = segb + (dj & 1) * kMaxPanelWidth;  // step dj's pivot row
+      // Header first: the column j+1 value (after the pending update), the
+      // row id, then the key with the pivot's sign.
       if (lane == 0) {
-        Tagged<T>::put_key(mine, ck, tag);
-        st_word(mine + 2, (unsigned int)ci, tag);
-        if (ck > 0) Tagged<T>::put(mine + 3, T(1) / S[cs * lds + j], tag);
+        K sgn = 0;
+        if (cs >= 0) {
+          if (j + 1 < w) {
+            T u1 = S[cs * lds + j + 1];
+            if (dj >= 0) u1 = upd<kExact>(u1, S[cs * lds + dj], up[j + 1]);
+            Tagged<T>::put(mine + Tagged<T>::kU1W, u1, tag);
+          }
+          if (signbit(S[cs * lds + j])) sgn = Tagged<T>::kSign;
+        }
+        st_word(mine + Tagged<T>::kIdW, (unsigned int)ci, tag);
+        Tagged<T>::put_key(mine, ck | sgn, tag);
       }
-      // Poll every CTA's header; fold each one in as soon as it is current.
-      K k = 0;
+      if (cs >= 0) {
+        if (dj >= 0) {
+          // The candidate row's pending update (lane 0 owns column j+1,
+          // which it read above), then its segment j+2...
+          const T l = S[cs * lds + dj];
+          for (int c = dj + 2 + lane; c < w; c += 32) S[cs * lds + c] = upd<kExact>(S[cs * lds + c], l, up[c]);
+          __syncwarp();
+        }
+        for (int c = j + 2 + lane; c < w; c += 32) Tagged<T>::put(mine + kHdr + c * kW, S[cs * lds + c], tag);
+      }
+      // Poll every CTA's header (32-byte loads); fold each one in as soon as
+      // it is current.  A positive key comes with its column j+1 value.
+      K k = 0, kraw = 0;
       int i = INT_MAX, win = -1;
+      T u1b = T(0);
       unsigned pending = 0;
       for (int q = 0; q < nq; ++q)
         if (lane + 32 * q < P) pending |= 1u << q;
-      const unsigned long long t0 = global_timer_ns();
+      t0 = global_timer_ns();
       unsigned int spins = 0;
       int ok = 1;
       while (true) {
@@ -377,11 +462,21 @@ __global__ void __launch_bounds__(256) panel_kernel(PanelArgs<T> p) {
           if (!(pending & (1u << q))) continue;
           const int cta = lane + 32 * q;
           const unsigned long long* h = slots + (size_t)cta * kPanelSlotWords;
-          K hk;
-          const bool kok = Tagged<T>::get_key(h, tag, hk);
-          const unsigned long long hi = ld_word(h + 2);
-          if (kok && word_ok(hi, tag)) {
-            key_combine(k, i, win, hk, (int)(unsigned int)hi, cta);
+          unsigned long long hw[4 * Tagged<T>::kHdrQuads];
+#pragma unroll
+          for (int v = 0; v < Tagged<T>::kHdrQuads; ++v) ld_quad(h + 4 * v, hw + 4 * v);
+          const K hraw = Tagged<T>::bits(hw);
+          const K hk = hraw & ~Tagged<T>::kSign;
+          if (Tagged<T>::ok(hw, tag) && word_ok(hw[Tagged<T>::kIdW], tag) &&
+              (hk == 0 || j + 1 >= w || Tagged<T>::ok(hw + Tagged<T>::kU1W, tag))) {
+            const int hid = (int)(unsigned int)hw[Tagged<T>::kIdW];
+            if (hk > k || (hk == k && hid < i)) {
+              k = hk;
+              i = hid;
+              win = cta;
+              kraw = hraw;
+              u1b = Tagged<T>::value(hw + Tagged<T>::kU1W);
+            }
             pending &= ~(1u << q);
           }
         }
@@ -394,57 +489,45 @@ __global__ void __launch_bounds__(256) panel_kernel(PanelArgs<T> p) {
       }
       int ret = -1;
       if (ok) {
-        key_reduce_warp<T>(k, i, win, 32);
+        const int src = key_reduce_redux(k, i, win);
+        const K praw = PivotKey<T>::shfl(kraw, src);
+        const T u1 = __shfl_sync(kFull, u1b, src);
         const int pr = (k > 0) ? i : ul;
         if (k > 0) {
-          // The pivot row's columns j.. and 1/pivot from the winner's slot.
-          const unsigned long long* ws = slots + (size_t)win * kPanelSlotWords;
-          while (true) {
-            bool got = true;
-            for (int c = j + lane; c < w; c += 32) {
-              T x;
-              got = Tagged<T>::get(ws + kHdr + c * kW, tag, x) && got;
-              seg[c] = x;
-            }
-            if (lane == 0) {
-              T rc;
-              got = Tagged<T>::get(ws + 3, tag, rc) && got;
-              s_recip = rc;
-            }
-            if (__all_sync(kFull, got)) break;
-            if (panel_wait_over(p.st, t0)) {
-              if (lane == 0 && !ld_relaxed_i32(&p.st->abort)) panel_give_up(p.st, ul);
-              ok = 0;
-              break;
-            }
+          // Start the copy of the winner's segment j+2.. (whole 16-byte
+          // pairs of its slot's words) into stage; it completes while the
+          // step goes on.
+          wseg = slots + (size_t)win * kPanelSlotWords + kHdr;
+          const int o0 = ((j + 2) * kW) & ~1, o1 = (w * kW + 1) & ~1;
+          seg_live = o1 > o0;
+          for (int o = o0 + 2 * lane; o < o1; o += 64) cp_async16(stage + o, wseg + o);
+          cp_async_commit();
+          if (lane == 0) {
+            s_recip = T(1) / PivotKey<T>::value(praw);
+            s_u1 = u1;
           }
         } else if (b == 0 && lane == 0) {
           // lair: max == 0 -> the step is singular, no swap, no update
           // (src/lapack/getrf.rs:72-73).  The last such step wins.
           atomicMax(&p.st->singular, ul);
         }
-        if (ok) {
-          // Relabel: the row with id ul takes id pr and the row with id pr
-          // takes id ul; the latter (the pivot row) retires after the barrier.
-          int found = 0;
-          for (int r = s_r0 + lane; r < nloc; r += 32) {
-            const int id = ids[r];
-            if (id == ul) found |= (r + 1) << 16;
-            if (id == pr) found |= r + 1;
+        // Relabel: the row with id ul takes id pr and the row with id pr
+        // takes id ul; the latter (the pivot row) retires after the barrier.
+        // Row pr is the winning CTA's candidate (slot cs); row ul's slot
+        // comes from the map of the panel's pending row ids.
+        const int s_ul = ulslot[j];
+        ret = s_ul;
+        if (pr != ul) {
+          const int s_pr = (win == b) ? cs : -1;
+          if (lane == 0) {
+            if (s_ul >= 0) ids[s_ul] = pr;
+            if (s_pr >= 0) ids[s_pr] = ul;
+            if (pr < p.k0 + w) ulslot[pr - p.k0] = s_ul;
           }
-          found = __reduce_or_sync(kFull, found);
-          const int s_ul = (found >> 16) - 1, s_pr = (found & 0xffff) - 1;
-          ret = s_ul;
-          if (pr != ul) {
-            if (lane == 0) {
-              if (s_ul >= 0) ids[s_ul] = pr;
-              if (s_pr >= 0) ids[s_pr] = ul;
-            }
-            ret = s_pr;
-          }
-          if (b == 0 && lane == 0) p.piv[ul] = pr;
-          if (lane == 0) s_pivoted = k > 0 ? 1 : 0;
+          ret = s_pr;
         }
+        if (b == 0 && lane == 0) p.piv[ul] = pr;
+        if (lane == 0) s_pivoted = k > 0 ? 1 : 0;
       }
       if (lane == 0) {
         s_ok = ok;
@@ -468,7 +551,9 @@ __global__ void __launch_bounds__(256) panel_kernel(PanelArgs<T> p) {
         }
         if (lane == 0) {
           const int t = ids[ret];
-          ids[ret] = ids[r0];
+          const int moved = ids[r0];  // this row now lives in slot ret
+          if (moved > ul && moved < p.k0 + w) ulslot[moved - p.k0] = ret;
+          ids[ret] = moved;
           ids[r0] = t;
           const int o = orig[ret];
           orig[ret] = orig[r0];
@@ -487,7 +572,7 @@ __global__ void __launch_bounds__(256) panel_kernel(PanelArgs<T> p) {
       const T recip = s_recip;
       for (int r = r0 + tid; r < nloc; r += blockDim.x) S[r * lds + j] = mul_rn(S[r * lds + j], recip);
       if (j + 1 < w) {
-        const T u1 = seg[j + 1];
+        const T u1 = s_u1;
         for (int r = r0 + tid; r < nloc; r += blockDim.x) {
           const T v = upd<kExact>(S[r * lds + j + 1], S[r * lds + j], u1);
           S[r * lds + j + 1] = v;
@@ -502,13 +587,41 @@ __global__ void __launch_bounds__(256) panel_kernel(PanelArgs<T> p) {
           key_combine(bk, bi, bs, PivotKey<T>::of(S[r * lds + j + 1]), ids[r], r);
       dj = -1;
     }
-    key_reduce_warp<T>(bk, bi, bs, 32);
+    key_reduce_redux(bk, bi, bs);
     if (lane == 0) {
       red_k[warp] = bk;
       red_i[warp] = bi;
       red_s[warp] = bs;
     }
+    if (warp == 0 && seg_live) {
+      // The winner's segment from stage into the pivot-row buffer; a word
+      // whose tag is not yet this step's (relaxed stores land in any order)
+      // is read again.
+      cp_async_wait_all();
+      __syncwarp();
+      bool got = true;
+      while (got) {
+        for (int c = j + 2 + lane; c < w; c += 32) {
+          unsigned long long* sw = stage + c * kW;
+          if (Tagged<T>::ok(sw, tag)) {
+            seg[c] = Tagged<T>::value(sw);
+          } else {
+#pragma unroll
+            for (int e = 0; e < kW; ++e) sw[e] = ld_word(wseg + c * kW + e);
+            got = false;
+          }
+        }
+        if (__all_sync(kFull, got)) break;
+        got = true;
+        if (panel_wait_over(p.st, t0)) got = false;
+      }
+      if (!got && lane == 0) {
+        if (!ld_relaxed_i32(&p.st->abort)) panel_give_up(p.st, ul);
+        s_ok = 0;
+      }
+    }
     __syncthreads();
+    if (!s_ok) return;
   }
   for (int idx = tid; idx < nloc * w; idx += blockDim.x) {
     const int r = idx / w, c = idx - r * w;
@@ -788,8 +901,6 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem, int src
   const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(src_bytes) : "memory");
 }
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
 __global__ void __launch_bounds__(256, 1) gemm_dmma_persistent_kernel(double* a, int64_t lda, int r0, int c0,
                                                                       int kk0, int K, int M, int N) {
@@ -908,16 +1019,33 @@ __global__ void __launch_bounds__(256, 1) gemm_dmma_persistent_kernel(double* a,
 // ---------------------------------------------------------------------------
 // Host driver.
 // ---------------------------------------------------------------------------
+// Shared-memory row stride of the panel: FP64 w + 1 (conflict-free column
+// access); FP32 rows padded to a multiple of 4 floats plus 4, so every row
+// starts on 16 bytes for the float4 look-ahead (column access then has
+// 4-way bank conflicts, a small cost on two columns a step).
+template <typename T>
+static int panel_lds(int w) {
+  return sizeof(T) == 4 ? ((w + 3) & ~3) + 4 : w + 1;
+}
+// Threads of a panel CTA: FP32 uses 16 warps so the look-ahead's shared-memory
+// latency is hidden; FP64's look-ahead is bound by the FP64 pipe.
+template <typename T>
+static int panel_threads() {
+  return sizeof(T) == 4 ? 512 : 256;
+}
 template <typename T>
 static size_t panel_smem_bytes(int rows_per, int w) {
-  return ((size_t)rows_per * (w + 1) + 2 * kMaxPanelWidth) * sizeof(T) + 2 * (size_t)rows_per * sizeof(int);
+  return ((size_t)rows_per * panel_lds<T>(w) + 2 * kMaxPanelWidth) * sizeof(T) + 2 * (size_t)rows_per * sizeof(int);
 }
 
 template <typename T, bool kExact>
 static int launch_panel(luhot_ctx* ctx, T* a, int64_t lda, int m, int k0, int w, int* piv,
                         cudaStream_t stream) {
   const int rows = m - k0;
-  const int max_smem = ctx->max_smem_optin;
+  auto kern = panel_kernel<T, kExact>;
+  cudaFuncAttributes fa;
+  LUHOT_CUDA_TRY(ctx, cudaFuncGetAttributes(&fa, kern));
+  const int max_smem = ctx->max_smem_optin - (int)fa.sharedSizeBytes;  // less the static exchange buffers
   // CTAs: enough that each owns >= 32 rows, at most pmax (raised up to the
   // SM count when the rows of one CTA would not fit in shared memory).
   // The exchange latency per column grows with P; FP32 panels (whose
@@ -933,11 +1061,10 @@ static int launch_panel(luhot_ctx* ctx, T* a, int64_t lda, int m, int k0, int w,
   if (panel_smem_bytes<T>(rows_per, w) > (size_t)max_smem)
     return set_error(ctx, LUHOT_ERR_UNSUPPORTED, "panel does not fit in shared memory");
   const size_t smem = panel_smem_bytes<T>(rows_per, w);
-  auto kern = panel_kernel<T, kExact>;
   LUHOT_CUDA_TRY(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)smem));
   int per_sm = 0;
-  LUHOT_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, smem));
+  LUHOT_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, panel_threads<T>(), smem));
   if (per_sm * ctx->num_sms < P)
     return set_error(ctx, LUHOT_ERR_UNSUPPORTED, "panel grid cannot be co-resident");
   PanelArgs<T> args;
@@ -947,7 +1074,7 @@ static int launch_panel(luhot_ctx* ctx, T* a, int64_t lda, int m, int k0, int w,
   args.k0 = k0;
   args.w = w;
   args.rows_per = rows_per;
-  args.lds = w + 1;
+  args.lds = panel_lds<T>(w);
   args.piv = piv;
   args.slots = static_cast<unsigned long long*>(ctx->panel_scratch);
   args.moves = reinterpret_cast<int*>(static_cast<char*>(ctx->panel_scratch) + kPanelSlotBytes);
@@ -956,7 +1083,7 @@ static int launch_panel(luhot_ctx* ctx, T* a, int64_t lda, int m, int k0, int w,
   LUHOT_CUDA_TRY(ctx, cudaMemsetAsync(args.move_count, 0, sizeof(int), stream));
   void* kargs[] = {&args};
   prof_begin(ctx, kProfPanel);
-  LUHOT_CUDA_TRY(ctx, cudaLaunchCooperativeKernel((void*)kern, dim3(P), dim3(256), kargs, smem,
+  LUHOT_CUDA_TRY(ctx, cudaLaunchCooperativeKernel((void*)kern, dim3(P), dim3(panel_threads<T>()), kargs, smem,
                                                   stream));
   // panel flops: sum over steps of (rows below) * (1 + 2 * cols right)
   double fl = 0.0;

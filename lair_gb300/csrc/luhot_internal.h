@@ -19,11 +19,14 @@ constexpr int kMaxPanelCtas = 256;     // >= SM count
 constexpr int kDefaultPanelWidth = 64; // FP64 / FP32 CUDA-core and DMMA paths
 constexpr int kTcPanelWidth = 128;     // tensor-core (tcgen05) Schur-update path
 constexpr int kMaxPanelWidth = 128;    // sizes the panel kernel's scratch
-// Panel exchange slots: per step parity and CTA, a 6-word header (pivot key,
-// row id, reciprocal) and the candidate row segment, in 8-byte words of
-// (payload, step tag), two words per FP64 value.
-constexpr int kPanelHeaderWords = 6;
+// Panel exchange slots: per step parity and CTA, an 8-word header (FP32:
+// signed pivot key at 0, row id at 1, the candidate's next-column value at 2;
+// FP64: key at 0-1, id at 2, next-column value at 3-4) and the candidate row
+// segment from word 8, in 8-byte words of (payload, step tag), two words per
+// FP64 value.
+constexpr int kPanelHeaderWords = 8;
 constexpr int kPanelSlotWords = kPanelHeaderWords + 2 * kMaxPanelWidth;
+static_assert(kPanelSlotWords % 4 == 0, "panel slots are whole 32-byte sectors (32-byte header loads)");
 constexpr size_t kPanelSlotBytes = 2 * (size_t)kMaxPanelCtas * kPanelSlotWords * sizeof(unsigned long long);
 // Followed by the panel's row moves: up to 2 * kMaxPanelWidth (destination,
 // source) pairs and their count.
