@@ -229,6 +229,46 @@ int trsv_scratch(luhot_ctx* ctx, int n, int** flags, int** ticket) {
 }
 
 template <typename T>
+int trsv_chain_sweep(luhot_ctx* ctx, const float* lu, int64_t lda, T* x, int n, bool lower, const T* dinv) {
+  const size_t words = trsv_chain_tag_words(n);
+  const size_t bytes = words * sizeof(unsigned long long) + 256;
+  if (ctx->chain_buf.bytes < bytes) {
+    int rc = ensure_buf(ctx, ctx->chain_buf, bytes);
+    if (rc) return rc;
+    LUHOT_CUDA_TRY(ctx, cudaMemsetAsync(ctx->chain_buf.ptr, 0, ctx->chain_buf.bytes, ctx->stream));
+    ctx->chain_epoch = 0;
+  }
+  auto* xt = static_cast<unsigned long long*>(ctx->chain_buf.ptr);
+  int* ticket = reinterpret_cast<int*>(xt + words);
+  if (++ctx->chain_epoch == 0) {  // the tag wrapped: clear every word once
+    LUHOT_CUDA_TRY(ctx, cudaMemsetAsync(xt, 0, words * sizeof(unsigned long long), ctx->stream));
+    ctx->chain_epoch = 1;
+  }
+  prof_begin(ctx, kProfTrsv);
+  cudaError_t e = launch_trsv_chain<T>(ctx->stream, lu, lda, x, n, lower, dinv, xt, ctx->chain_epoch, ticket,
+                                       ctx->d_status);
+  prof_end(ctx, kProfTrsv, (double)n * n, (double)n * n / 2 * sizeof(float) + 2.0 * n * sizeof(T));
+  count_launch(ctx);
+  if (e != cudaSuccess) return set_error(ctx, LUHOT_ERR_CUDA, std::string("chained sweep: ") + cudaGetErrorString(e));
+  return LUHOT_OK;
+}
+
+template <typename T>
+int chain_invert_blocks(luhot_ctx* ctx, int n, const float* lu, int64_t lda, T* dinv_l, T* dinv_u) {
+  prof_begin(ctx, kProfTrsv);
+  cudaError_t e = launch_trsv_chain_invert<T>(ctx->stream, lu, lda, n, true, dinv_l);
+  if (e == cudaSuccess) e = launch_trsv_chain_invert<T>(ctx->stream, lu, lda, n, false, dinv_u);
+  prof_end(ctx, kProfTrsv, 2.0 * 128.0 * 128.0 * 128.0 / 3.0 * trsv_chain_blocks(n),
+           4.0 * (double)trsv_chain_inverse_elems(n) * sizeof(T));
+  count_launch(ctx, 2);
+  if (e != cudaSuccess) return set_error(ctx, LUHOT_ERR_CUDA, std::string("diagonal inverses: ") + cudaGetErrorString(e));
+  return LUHOT_OK;
+}
+
+template int trsv_chain_sweep<float>(luhot_ctx*, const float*, int64_t, float*, int, bool, const float*);
+template int chain_invert_blocks<float>(luhot_ctx*, int, const float*, int64_t, float*, float*);
+
+template <typename T>
 int getrs_apply(luhot_ctx* ctx, int n, int nrhs, const T* lu, int64_t lda, const int* perm, const T* b,
                 int64_t ldb, T* x, int64_t ldx, int trans, int mode, T* w, const T* dinv_l, const T* dinv_u) {
   cudaStream_t stream = ctx->stream;

@@ -102,7 +102,8 @@ __global__ void ir_matvec_kernel(const double* __restrict__ a, int64_t lda, cons
 }
 
 // out[i] = v[perm[i]] (P^T v).
-__global__ void ir_gather_kernel(const double* __restrict__ v, const int* __restrict__ perm, double* out, int n) {
+template <typename T>
+__global__ void ir_gather_kernel(const T* __restrict__ v, const int* __restrict__ perm, T* out, int n) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = v[perm[i]];
 }
 
@@ -266,13 +267,15 @@ struct IrRun {
   // arithmetic on FP64 vectors (no rounding of the Krylov vectors): the
   // preconditioner of GMRES-IR, whose accuracy then depends only on the
   // factors, not on u_low * kappa of each application.
+  // FP64 arithmetic is slow on this part, so these sweeps keep 64-row
+  // blocks (a quarter of the per-step FP64 work of the chained 128-row form).
   int lo_solve64(const double* v, double* out) {
     int* flags = nullptr;
     int* ticket = nullptr;
     int rc = trsv_scratch(ctx, n, &flags, &ticket);
     if (rc) return rc;
     prof_begin(ctx, kProfRefine);
-    ir_gather_kernel<<<grid_vec, 256, 0, ctx->stream>>>(v, perm, out, n);
+    ir_gather_kernel<double><<<grid_vec, 256, 0, ctx->stream>>>(v, perm, out, n);
     prof_end(ctx, kProfRefine, 0.0, 20.0 * n);
     prof_begin(ctx, kProfTrsv);
     cudaError_t e = launch_trsv_syncfree<double, Tlo>(ctx->stream, lu, ldlo, out, 1, n, 1, true, true, false, false,
@@ -296,7 +299,13 @@ struct IrRun {
     prof_end(ctx, kProfRefine, 0.0, (8.0 + sizeof(Tlo)) * n);
     rc = launch_check("ir to-low");
     if (rc) return rc;
-    rc = getrs_apply<Tlo>(ctx, n, 1, lu, ldlo, perm, lo1, 1, lo2, 1, 0, LUHOT_MODE_FAST, low, dl, du);
+    // lo2 = P lo1, then L and U sweeps in place (chained, 128-row blocks).
+    prof_begin(ctx, kProfPermute);
+    ir_gather_kernel<Tlo><<<grid_vec, 256, 0, ctx->stream>>>(lo1, perm, lo2, n);
+    prof_end(ctx, kProfPermute, 0.0, (4.0 + 2.0 * sizeof(Tlo)) * n);
+    rc = launch_check("ir gather");
+    if (!rc) rc = trsv_chain_sweep<Tlo>(ctx, lu, ldlo, lo2, n, true, dl);
+    if (!rc) rc = trsv_chain_sweep<Tlo>(ctx, lu, ldlo, lo2, n, false, du);
     if (rc) return rc;
     prof_begin(ctx, kProfRefine);
     if (add_into_out) {
@@ -472,17 +481,18 @@ static int ir_factor(IrRun<float>& s, int precision, luhot_ir_info* info) {
   if (rc) return rc;
   info->singular = sing;
   if (sing >= 0) return set_error(ctx, LUHOT_ERR_SINGULAR, "the low-precision factor is singular");
-  // Inverses of the diagonal blocks for the sweeps of every later solve, in
-  // the factor's precision (plain IR) and widened to FP64 (GMRES-IR).
-  const size_t ne = trsv_inverse_elems(n);
-  rc = ensure_buf(ctx, ctx->dinv_buf, 2 * ne * (sizeof(double) + sizeof(float)));
+  // Inverses of the diagonal blocks for the sweeps of every later solve: the
+  // 128 x 128 blocks of the chained FP32 sweeps (plain IR) and the 64 x 64
+  // blocks widened to FP64 (GMRES-IR's preconditioner).
+  const size_t ne64 = trsv_inverse_elems(n), ne = trsv_chain_inverse_elems(n);
+  rc = ensure_buf(ctx, ctx->dinv_buf, 2 * ne64 * sizeof(double) + 2 * ne * sizeof(float));
   if (rc) return rc;
   s.dl64 = static_cast<double*>(ctx->dinv_buf.ptr);
-  s.du64 = s.dl64 + ne;
-  s.dl = reinterpret_cast<float*>(s.du64 + ne);
+  s.du64 = s.dl64 + ne64;
+  s.dl = reinterpret_cast<float*>(s.du64 + ne64);
   s.du = s.dl + ne;
   rc = invert_diag_blocks<double, float>(ctx, n, s.lu, s.ldlo, s.dl64, s.du64);
-  if (!rc) rc = invert_diag_blocks<float, float>(ctx, n, s.lu, s.ldlo, s.dl, s.du);
+  if (!rc) rc = chain_invert_blocks<float>(ctx, n, s.lu, s.ldlo, s.dl, s.du);
   if (rc) return rc;
   return getrs_perm(ctx, s.piv, n, s.perm);
 }

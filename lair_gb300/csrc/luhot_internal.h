@@ -79,6 +79,8 @@ struct luhot_ctx {
   luhot::DevBuf adj_buf;                    // adjoint: A^T or dA
   luhot::DevBuf tc_buf;                     // tensor-core LU: operand copies + scales
   luhot::DevBuf dinv_buf;                   // inverses of the 64 x 64 diagonal blocks of L and U
+  luhot::DevBuf chain_buf;                  // chained sweeps: tagged x words + ticket
+  unsigned int chain_epoch = 0;             // tag of the last chained sweep (0 = none)
   double* h_scalars = nullptr;              // pinned: scalars read back by the refinement loop
   void* h_piv = nullptr;                    // pinned pivots staging
   size_t h_piv_bytes = 0;
@@ -136,6 +138,14 @@ int getrs_device(luhot_ctx* ctx, int n, int nrhs, const T* lu, int64_t lda, cons
 int getrs_perm(luhot_ctx* ctx, const int* piv, int n, int* perm);
 // Ready flags and ticket of the sync-free triangular sweeps for order n.
 int trsv_scratch(luhot_ctx* ctx, int n, int** flags, int** ticket);
+// One chained sweep (launch_trsv_chain) on the context's stream with a fresh
+// epoch and the context's tagged-word scratch.
+template <typename T>
+int trsv_chain_sweep(luhot_ctx* ctx, const float* lu, int64_t lda, T* x, int n, bool lower, const T* dinv);
+// Inverses of the 128 x 128 diagonal blocks of L and U of an FP32 factor in
+// the arithmetic type T (trsv_chain_inverse_elems(n) elements each).
+template <typename T>
+int chain_invert_blocks(luhot_ctx* ctx, int n, const float* lu, int64_t lda, T* dinv_l, T* dinv_u);
 template <typename T>
 int getrs_apply(luhot_ctx* ctx, int n, int nrhs, const T* lu, int64_t lda, const int* perm, const T* b,
                 int64_t ldb, T* x, int64_t ldx, int trans, int mode, T* w, const T* dinv_l = nullptr,

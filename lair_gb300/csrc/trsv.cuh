@@ -31,4 +31,19 @@ size_t trsv_inverse_elems(int n);
 template <typename T, typename TA = T>
 cudaError_t launch_trsv_invert_diag(cudaStream_t stream, const TA* a, int64_t lda, int n, bool lower, T* dinv);
 
+// Chained sweep for one right-hand side with FP32 factors (trsv_chain.cu):
+// 128-row blocks publishing x as epoch-tagged words.  dinv holds the inverses
+// of the 128 x 128 diagonal blocks (launch_trsv_chain_invert); xt
+// trsv_chain_tag_words(n) words of device scratch zeroed once, then reused
+// with a new nonzero epoch per launch; ticket one int (cleared here).
+int trsv_chain_blocks(int n);
+size_t trsv_chain_inverse_elems(int n);
+size_t trsv_chain_tag_words(int n);
+template <typename T>
+cudaError_t launch_trsv_chain_invert(cudaStream_t stream, const float* a, int64_t lda, int n, bool lower, T* dinv);
+template <typename T>
+cudaError_t launch_trsv_chain(cudaStream_t stream, const float* a, int64_t lda, T* x, int n, bool lower,
+                              const T* dinv, unsigned long long* xt, unsigned int epoch, int* ticket,
+                              DeviceStatus* st);
+
 }  // namespace luhot
