@@ -331,18 +331,19 @@ __device__ __forceinline__ void panel_update(T* S, int lds, int r0, int nloc, in
 // to columns j+1.. still pending for all rows but this CTA's candidate row:
 //   warp 0:     publish the candidate's header (key = |pivot| bits with the
 //               pivot's sign on top, row id, column j+1 value after the
-//               pending update), then finish the candidate row's pending
-//               update and publish its segment j+2.., all as tagged words;
-//               poll the P headers until all carry this step's tag, folding
-//               them into the winner (the pivot and its column j+1 value come
-//               with its header); start the copy of the winner's segment into
-//               shared memory (cp.async); relabel the ids of rows ul and pr.
-//   warps 1-7:  meanwhile, the pending update of step j-1 (columns j+1..),
-//               which thus overlaps the exchange.
-//   barrier;    the pivot row's CTA retires it; all warps scale column j,
-//               update column j+1 only and find its candidates; warp 0 checks
-//               the copied segment's tags and keeps it for the next step's
-//               updates; barrier.
+//               pending update) as tagged words; poll the P headers until all
+//               carry this step's tag, folding them into the winner (the
+//               pivot and its column j+1 value come with its header); start
+//               the copy of the winner's segment into shared memory
+//               (cp.async); relabel the ids of rows ul and pr.
+//   warp 1:     meanwhile, the candidate row's pending update (columns
+//               j+2..) and the publication of its segment j+2..;
+//   warps 1-:   the pending update of step j-1 of the other rows (columns
+//               j+1..), which thus overlaps the exchange.
+//   barrier;    the pivot row's CTA retires it; warps 1- scale column j,
+//               update column j+1 only and find its candidates while warp 0
+//               checks the copied segment's tags and keeps it for the next
+//               step's updates; barrier.
 // The arithmetic and its order per element are those of lair's
 // getrf_row_major (src/lapack/getrf.rs:56-89): 1/p rounded, l = a*(1/p)
 // rounded, a - l*u (separately rounded in exact mode), steps in order.
@@ -421,30 +422,24 @@ __global__ void __launch_bounds__(512, 1) panel_kernel(PanelArgs<T> p) {
     if (warp == 0) {
       unsigned long long* mine = slots + (size_t)b * kPanelSlotWords;
       const T* up = segb + (dj & 1) * kMaxPanelWidth;  // step dj's pivot row
-      // Header first: the column j+1 value (after the pending update), the
-      // row id, then the key with the pivot's sign.
+      // The header only (warp 1 publishes the segment): the column j+1 value
+      // after the pending update (kept in the row), the row id, then the key
+      // with the pivot's sign.
       if (lane == 0) {
         K sgn = 0;
         if (cs >= 0) {
           if (j + 1 < w) {
             T u1 = S[cs * lds + j + 1];
-            if (dj >= 0) u1 = upd<kExact>(u1, S[cs * lds + dj], up[j + 1]);
+            if (dj >= 0) {
+              u1 = upd<kExact>(u1, S[cs * lds + dj], up[j + 1]);
+              S[cs * lds + j + 1] = u1;
+            }
             Tagged<T>::put(mine + Tagged<T>::kU1W, u1, tag);
           }
           if (signbit(S[cs * lds + j])) sgn = Tagged<T>::kSign;
         }
         st_word(mine + Tagged<T>::kIdW, (unsigned int)ci, tag);
         Tagged<T>::put_key(mine, ck | sgn, tag);
-      }
-      if (cs >= 0) {
-        if (dj >= 0) {
-          // The candidate row's pending update (lane 0 owns column j+1,
-          // which it read above), then its segment j+2...
-          const T l = S[cs * lds + dj];
-          for (int c = dj + 2 + lane; c < w; c += 32) S[cs * lds + c] = upd<kExact>(S[cs * lds + c], l, up[c]);
-          __syncwarp();
-        }
-        for (int c = j + 2 + lane; c < w; c += 32) Tagged<T>::put(mine + kHdr + c * kW, S[cs * lds + c], tag);
       }
       // Poll every CTA's header (32-byte loads); fold each one in as soon as
       // it is current.  A positive key comes with its column j+1 value.
@@ -533,9 +528,22 @@ __global__ void __launch_bounds__(512, 1) panel_kernel(PanelArgs<T> p) {
         s_ok = ok;
         s_ret = ret;
       }
-    } else if (dj >= 0) {
-      panel_update<T, kExact>(S, lds, dr0, nloc, cs, dj, dj + 2, w, segb + (dj & 1) * kMaxPanelWidth, tid - 32,
-                              blockDim.x - 32);
+    } else {
+      if (warp == 1 && cs >= 0) {
+        // The candidate row's pending update of columns j+2.. (warp 0 did
+        // column j+1), then its segment j+2.., while warp 0 polls.
+        unsigned long long* mine = slots + (size_t)b * kPanelSlotWords;
+        if (dj >= 0) {
+          const T* up = segb + (dj & 1) * kMaxPanelWidth;
+          const T l = S[cs * lds + dj];
+          for (int c = dj + 3 + lane; c < w; c += 32) S[cs * lds + c] = upd<kExact>(S[cs * lds + c], l, up[c]);
+          __syncwarp();
+        }
+        for (int c = j + 2 + lane; c < w; c += 32) Tagged<T>::put(mine + kHdr + c * kW, S[cs * lds + c], tag);
+      }
+      if (dj >= 0)
+        panel_update<T, kExact>(S, lds, dr0, nloc, cs, dj, dj + 2, w, segb + (dj & 1) * kMaxPanelWidth, tid - 32,
+                                blockDim.x - 32);
     }
     __syncthreads();
     if (!s_ok) return;
@@ -565,35 +573,30 @@ __global__ void __launch_bounds__(512, 1) panel_kernel(PanelArgs<T> p) {
       if (tid == 0) s_r0 = r0;
     }
 
-    // Scale column j, update column j+1 only, find its candidates.
+    // Warps 1-: scale column j, update column j+1 only, find its candidates.
+    // Warp 0 meanwhile keeps the winner's segment for the next step.
     K bk = 0;
     int bi = INT_MAX, bs = -1;
-    if (s_pivoted) {
-      const T recip = s_recip;
-      for (int r = r0 + tid; r < nloc; r += blockDim.x) S[r * lds + j] = mul_rn(S[r * lds + j], recip);
-      if (j + 1 < w) {
-        const T u1 = s_u1;
-        for (int r = r0 + tid; r < nloc; r += blockDim.x) {
-          const T v = upd<kExact>(S[r * lds + j + 1], S[r * lds + j], u1);
-          S[r * lds + j + 1] = v;
-          key_combine(bk, bi, bs, PivotKey<T>::of(v), ids[r], r);
+    const int pivoted = s_pivoted;
+    if (warp != 0) {
+      const int t1 = tid - 32, n1 = blockDim.x - 32;
+      if (pivoted) {
+        const T recip = s_recip;
+        for (int r = r0 + t1; r < nloc; r += n1) S[r * lds + j] = mul_rn(S[r * lds + j], recip);
+        if (j + 1 < w) {
+          const T u1 = s_u1;
+          for (int r = r0 + t1; r < nloc; r += n1) {
+            const T v = upd<kExact>(S[r * lds + j + 1], S[r * lds + j], u1);
+            S[r * lds + j + 1] = v;
+            key_combine(bk, bi, bs, PivotKey<T>::of(v), ids[r], r);
+          }
         }
-      }
-      dj = j;
-      dr0 = r0;
-    } else {
-      if (j + 1 < w)
-        for (int r = r0 + tid; r < nloc; r += blockDim.x)
+      } else if (j + 1 < w) {
+        for (int r = r0 + t1; r < nloc; r += n1)
           key_combine(bk, bi, bs, PivotKey<T>::of(S[r * lds + j + 1]), ids[r], r);
-      dj = -1;
-    }
-    key_reduce_redux(bk, bi, bs);
-    if (lane == 0) {
-      red_k[warp] = bk;
-      red_i[warp] = bi;
-      red_s[warp] = bs;
-    }
-    if (warp == 0 && seg_live) {
+      }
+      key_reduce_redux(bk, bi, bs);
+    } else if (seg_live) {
       // The winner's segment from stage into the pivot-row buffer; a word
       // whose tag is not yet this step's (relaxed stores land in any order)
       // is read again.
@@ -620,6 +623,13 @@ __global__ void __launch_bounds__(512, 1) panel_kernel(PanelArgs<T> p) {
         s_ok = 0;
       }
     }
+    if (lane == 0) {
+      red_k[warp] = bk;
+      red_i[warp] = bi;
+      red_s[warp] = bs;
+    }
+    dj = pivoted ? j : -1;
+    dr0 = r0;
     __syncthreads();
     if (!s_ok) return;
   }
