@@ -662,17 +662,34 @@ __global__ void __launch_bounds__(256) laswp_moves_kernel(T* a, int64_t lda, con
                                                           int c_right_begin, int n) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* vals = reinterpret_cast<T*>(smem_raw);  // [capacity][32]
-  const int count = min(*move_count, capacity);
+  __shared__ int mv[4 * kMaxPanelWidth];      // the (destination, source) pairs
+  const int count = min(min(*move_count, capacity), 2 * kMaxPanelWidth);
+  const int tid = threadIdx.y * 32 + threadIdx.x;
+  for (int i = tid; i < 2 * count; i += blockDim.x * blockDim.y) mv[i] = moves[i];
+  __syncthreads();
   const int nleft = c_left_end;
   const int t = blockIdx.x * 32 + threadIdx.x;
   const int nright = max(0, n - c_right_begin);
   const bool on = t < nleft + nright;
   const int c = (t < nleft) ? t : (c_right_begin + t - nleft);
-  for (int e = threadIdx.y; e < count; e += blockDim.y)
-    if (on) vals[e * 32 + threadIdx.x] = a[(int64_t)moves[2 * e + 1] * lda + c];
+  // Eight source rows per thread in flight before any is stored.
+  constexpr int kB = 8;
+  for (int e0 = threadIdx.y; e0 < count; e0 += blockDim.y * kB) {
+    T v[kB];
+#pragma unroll
+    for (int q = 0; q < kB; ++q) {
+      const int e = e0 + q * blockDim.y;
+      v[q] = (on && e < count) ? a[(int64_t)mv[2 * e + 1] * lda + c] : T(0);
+    }
+#pragma unroll
+    for (int q = 0; q < kB; ++q) {
+      const int e = e0 + q * blockDim.y;
+      if (on && e < count) vals[e * 32 + threadIdx.x] = v[q];
+    }
+  }
   __syncthreads();
   for (int e = threadIdx.y; e < count; e += blockDim.y)
-    if (on) a[(int64_t)moves[2 * e] * lda + c] = vals[e * 32 + threadIdx.x];
+    if (on) a[(int64_t)mv[2 * e] * lda + c] = vals[e * 32 + threadIdx.x];
 }
 
 
