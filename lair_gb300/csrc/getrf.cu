@@ -88,7 +88,6 @@ struct PivotKey<float> {
     const unsigned int b = __float_as_uint(x) & 0x7fffffffu;
     return b > 0x7f800000u ? 0u : b;
   }
-  __device__ static K shfl_xor(K k, int off) { return __shfl_xor_sync(0xffffffffu, k, off); }
   __device__ static K shfl(K k, int src) { return __shfl_sync(0xffffffffu, k, src); }
   __device__ static float value(K raw) { return __uint_as_float(raw); }
 };
@@ -99,7 +98,6 @@ struct PivotKey<double> {
     const unsigned long long b = (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
     return b > 0x7ff0000000000000ull ? 0ull : b;
   }
-  __device__ static K shfl_xor(K k, int off) { return __shfl_xor_sync(0xffffffffu, k, off); }
   __device__ static K shfl(K k, int src) { return __shfl_sync(0xffffffffu, k, src); }
   __device__ static double value(K raw) { return __longlong_as_double((long long)raw); }
 };

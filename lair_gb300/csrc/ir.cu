@@ -233,7 +233,6 @@ struct IrRun {
   int* perm;
   Tlo* lo1;
   Tlo* lo2;
-  Tlo* low;    // getrs scratch
   double* r;   // residual / Arnoldi work
   double* t;   // second FP64 work vector
   double* V;   // (restart + 1) x n
@@ -262,7 +261,6 @@ struct IrRun {
     return LUHOT_OK;
   }
 
-  // out (FP64) = (LU)^-1 v, through the low precision with infinity-norm scaling.
   // out (FP64) = (LU)^-1 v with the low-precision factors applied in FP64
   // arithmetic on FP64 vectors (no rounding of the Krylov vectors): the
   // preconditioner of GMRES-IR, whose accuracy then depends only on the
@@ -288,6 +286,9 @@ struct IrRun {
     return LUHOT_OK;
   }
 
+  // out (FP64) = (LU)^-1 v through the low precision with infinity-norm
+  // scaling (the plain-IR correction), or out += it: v scaled and rounded to
+  // FP32, permuted, the chained FP32 sweeps, widened back.
   int lo_solve(const double* v, double* out, bool add_into_out) {
     int rc = zero_scalar(kVscale);
     if (rc) return rc;
@@ -447,7 +448,6 @@ static int ir_setup(luhot_ctx* ctx, int n, const double* a, int64_t lda, IrRun<f
   s.V = s.t + n;
   s.lo1 = reinterpret_cast<float*>(s.V + (size_t)(kGmresRestart + 1) * n);
   s.lo2 = s.lo1 + n;
-  s.low = s.lo2 + n;
   s.piv = static_cast<int*>(ctx->ir_buf[2].ptr);
   s.perm = s.piv + n;
   s.sc = reinterpret_cast<double*>(s.piv + idx_ints);
