@@ -132,7 +132,7 @@ extern "C" int luhot_measure_dmma_peak(luhot_ctx* ctx, double* tflops) {
   cudaSetDevice(ctx->device);
   const int iters = 2048;
   double best = 0.0;
-  const int configs[][2] = {{4, 256}, {8, 256}, {2, 512}, {4, 128}};
+  const int launch_shapes[][2] = {{4, 256}, {8, 256}, {2, 512}, {4, 128}};
   double* out = nullptr;
   const size_t max_threads = (size_t)ctx->num_sms * 8 * 256;
   LUHOT_CUDA_TRY(ctx, cudaMalloc(&out, max_threads * sizeof(double)));
@@ -140,7 +140,7 @@ extern "C" int luhot_measure_dmma_peak(luhot_ctx* ctx, double* tflops) {
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   for (int rep = 0; rep < 2; ++rep) {
-    for (const auto& cfg : configs) {
+    for (const auto& cfg : launch_shapes) {
       const int blocks = ctx->num_sms * cfg[0], threads = cfg[1];
       cudaEventRecord(e0, ctx->stream);
       dmma_peak_kernel<<<blocks, threads, 0, ctx->stream>>>(out, 0.999, 1e-3, iters);
