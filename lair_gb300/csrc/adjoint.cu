@@ -113,6 +113,7 @@ extern "C" {
 int luhot_dgesv_backward_dev(luhot_ctx* ctx, int64_t n, int64_t nrhs, const double* d_lu, int64_t lda,
                              const int32_t* d_piv, const double* d_x, int64_t ldx, const double* d_w, int64_t ldw,
                              double* d_db, int64_t lddb, double* d_da, int64_t ldda, int mode) {
+  LUHOT_NVTX_FN();
   if (!ctx) return LUHOT_ERR_INVALID_ARG;
   CtxGuard g(ctx);
   if (n < 0 || nrhs < 0 || n >= INT32_MAX || nrhs >= INT32_MAX)
@@ -127,6 +128,7 @@ int luhot_dgesv_backward_ir_dev(luhot_ctx* ctx, int64_t n, int64_t nrhs, const d
                                 const double* d_x, int64_t ldx, const double* d_w, int64_t ldw, double* d_db,
                                 int64_t lddb, double* d_da, int64_t ldda, int precision, int solver, double tol,
                                 int max_iter, luhot_ir_info* info) {
+  LUHOT_NVTX_FN();
   if (!ctx || !info) return LUHOT_ERR_INVALID_ARG;
   CtxGuard g(ctx);
   if (n < 0 || nrhs < 0 || n >= INT32_MAX || nrhs >= INT32_MAX)
@@ -143,6 +145,7 @@ extern "C" int luhot_dgesv_backward(luhot_ctx* ctx, int64_t n, int64_t nrhs, con
                                     int64_t lu_cs, const uint64_t* piv, const double* x, int64_t x_rs, int64_t x_cs,
                                     const double* w, int64_t w_rs, int64_t w_cs, double* db, int64_t db_rs,
                                     int64_t db_cs, double* da, int64_t da_rs, int64_t da_cs, int mode) {
+  LUHOT_NVTX_FN();
   if (!ctx) return LUHOT_ERR_INVALID_ARG;
   CtxGuard g(ctx);
   if (n < 0 || nrhs < 0 || n >= INT32_MAX || nrhs >= INT32_MAX)

@@ -471,6 +471,7 @@ int luhot_selftest_wait_timeout(luhot_ctx* ctx, int64_t timeout_ms) {
 
 int luhot_dgetrf(luhot_ctx* ctx, int64_t m, int64_t n, double* a, int64_t rs, int64_t cs, uint64_t* piv,
                  int64_t* singular, int mode) {
+  LUHOT_NVTX_FN();
   if (!ctx) return LUHOT_ERR_INVALID_ARG;
   Guard g(ctx);
   return getrf_host<double>(ctx, m, n, a, rs, cs, piv, singular, mode);
@@ -478,6 +479,7 @@ int luhot_dgetrf(luhot_ctx* ctx, int64_t m, int64_t n, double* a, int64_t rs, in
 
 int luhot_sgetrf(luhot_ctx* ctx, int64_t m, int64_t n, float* a, int64_t rs, int64_t cs, uint64_t* piv,
                  int64_t* singular, int mode) {
+  LUHOT_NVTX_FN();
   if (!ctx) return LUHOT_ERR_INVALID_ARG;
   Guard g(ctx);
   return getrf_host<float>(ctx, m, n, a, rs, cs, piv, singular, mode);
@@ -486,6 +488,7 @@ int luhot_sgetrf(luhot_ctx* ctx, int64_t m, int64_t n, float* a, int64_t rs, int
 int luhot_dgetrs(luhot_ctx* ctx, int64_t n, int64_t nrhs, const double* lu, int64_t lu_rs, int64_t lu_cs,
                  const uint64_t* piv, const double* b, int64_t b_rs, int64_t b_cs, double* x, int64_t x_rs,
                  int64_t x_cs, int trans, int mode) {
+  LUHOT_NVTX_FN();
   if (!ctx) return LUHOT_ERR_INVALID_ARG;
   Guard g(ctx);
   return getrs_host<double>(ctx, n, nrhs, lu, lu_rs, lu_cs, piv, b, b_rs, b_cs, x, x_rs, x_cs, trans, mode);
@@ -494,6 +497,7 @@ int luhot_dgetrs(luhot_ctx* ctx, int64_t n, int64_t nrhs, const double* lu, int6
 int luhot_sgetrs(luhot_ctx* ctx, int64_t n, int64_t nrhs, const float* lu, int64_t lu_rs, int64_t lu_cs,
                  const uint64_t* piv, const float* b, int64_t b_rs, int64_t b_cs, float* x, int64_t x_rs,
                  int64_t x_cs, int trans, int mode) {
+  LUHOT_NVTX_FN();
   if (!ctx) return LUHOT_ERR_INVALID_ARG;
   Guard g(ctx);
   return getrs_host<float>(ctx, n, nrhs, lu, lu_rs, lu_cs, piv, b, b_rs, b_cs, x, x_rs, x_cs, trans, mode);
@@ -501,6 +505,7 @@ int luhot_sgetrs(luhot_ctx* ctx, int64_t n, int64_t nrhs, const float* lu, int64
 
 int luhot_dgesv(luhot_ctx* ctx, int64_t n, int64_t nrhs, const double* a, int64_t rs, int64_t cs,
                 const double* b, int64_t b_rs, int64_t b_cs, double* x, int64_t x_rs, int64_t x_cs, int mode) {
+  LUHOT_NVTX_FN();
   if (!ctx) return LUHOT_ERR_INVALID_ARG;
   Guard g(ctx);
   if (!dims_ok(n, nrhs) || !dims_ok(n, n)) return set_error(ctx, LUHOT_ERR_INVALID_ARG, "gesv: invalid dimensions");
@@ -536,6 +541,7 @@ int luhot_dgesv(luhot_ctx* ctx, int64_t n, int64_t nrhs, const double* a, int64_
 
 int luhot_dgetrf_dev(luhot_ctx* ctx, int64_t m, int64_t n, double* d_a, int64_t lda, int32_t* d_piv,
                      int64_t* singular, int mode) {
+  LUHOT_NVTX_FN();
   if (!ctx) return LUHOT_ERR_INVALID_ARG;
   Guard g(ctx);
   if (!dims_ok(m, n)) return set_error(ctx, LUHOT_ERR_INVALID_ARG, "getrf: invalid dimensions");
@@ -545,6 +551,7 @@ int luhot_dgetrf_dev(luhot_ctx* ctx, int64_t m, int64_t n, double* d_a, int64_t 
 
 int luhot_sgetrf_dev(luhot_ctx* ctx, int64_t m, int64_t n, float* d_a, int64_t lda, int32_t* d_piv,
                      int64_t* singular, int mode) {
+  LUHOT_NVTX_FN();
   if (!ctx) return LUHOT_ERR_INVALID_ARG;
   Guard g(ctx);
   if (!dims_ok(m, n)) return set_error(ctx, LUHOT_ERR_INVALID_ARG, "getrf: invalid dimensions");
@@ -554,6 +561,7 @@ int luhot_sgetrf_dev(luhot_ctx* ctx, int64_t m, int64_t n, float* d_a, int64_t l
 
 int luhot_dgetrs_dev(luhot_ctx* ctx, int64_t n, int64_t nrhs, const double* d_lu, int64_t lda,
                      const int32_t* d_piv, double* d_b, int64_t ldb, int trans, int mode) {
+  LUHOT_NVTX_FN();
   if (!ctx) return LUHOT_ERR_INVALID_ARG;
   Guard g(ctx);
   if (!dims_ok(n, nrhs)) return set_error(ctx, LUHOT_ERR_INVALID_ARG, "getrs: invalid dimensions");
@@ -563,6 +571,7 @@ int luhot_dgetrs_dev(luhot_ctx* ctx, int64_t n, int64_t nrhs, const double* d_lu
 
 int luhot_sgetrs_dev(luhot_ctx* ctx, int64_t n, int64_t nrhs, const float* d_lu, int64_t lda,
                      const int32_t* d_piv, float* d_b, int64_t ldb, int trans, int mode) {
+  LUHOT_NVTX_FN();
   if (!ctx) return LUHOT_ERR_INVALID_ARG;
   Guard g(ctx);
   if (!dims_ok(n, nrhs)) return set_error(ctx, LUHOT_ERR_INVALID_ARG, "getrs: invalid dimensions");
@@ -573,6 +582,7 @@ int luhot_sgetrs_dev(luhot_ctx* ctx, int64_t n, int64_t nrhs, const float* d_lu,
 int luhot_dgesv_ir_dev(luhot_ctx* ctx, int64_t n, int64_t nrhs, const double* d_a, int64_t lda,
                        const double* d_b, int64_t ldb, double* d_x, int64_t ldx, int precision, int solver,
                        double tol, int max_iter, luhot_ir_info* info) {
+  LUHOT_NVTX_FN();
   if (!ctx || !info) return LUHOT_ERR_INVALID_ARG;
   Guard g(ctx);
   if (!dims_ok(n, nrhs) || !dims_ok(n, n)) return set_error(ctx, LUHOT_ERR_INVALID_ARG, "gesv_ir: invalid dimensions");
@@ -583,6 +593,7 @@ int luhot_dgesv_ir_dev(luhot_ctx* ctx, int64_t n, int64_t nrhs, const double* d_
 int luhot_dgesv_ir(luhot_ctx* ctx, int64_t n, int64_t nrhs, const double* a, int64_t rs, int64_t cs,
                    const double* b, int64_t b_rs, int64_t b_cs, double* x, int64_t x_rs, int64_t x_cs, int precision,
                    int solver, double tol, int max_iter, luhot_ir_info* info) {
+  LUHOT_NVTX_FN();
   if (!ctx || !info) return LUHOT_ERR_INVALID_ARG;
   Guard g(ctx);
   if (!dims_ok(n, nrhs) || !dims_ok(n, n)) return set_error(ctx, LUHOT_ERR_INVALID_ARG, "gesv_ir: invalid dimensions");

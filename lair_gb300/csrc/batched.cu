@@ -426,6 +426,7 @@ using namespace luhot;
 extern "C" {
 
 int luhot_batch_create(luhot_ctx* ctx, int64_t count, const int32_t* sizes, int dtype, int mode, luhot_batch** out) {
+  LUHOT_NVTX_FN();
   if (!ctx || !out) return LUHOT_ERR_INVALID_ARG;
   CtxGuard g(ctx);
   *out = nullptr;
@@ -497,6 +498,7 @@ int luhot_batch_tuning(const luhot_batch* p, int32_t* nb_per_bucket, int32_t* sm
 }
 
 int luhot_batch_solve(luhot_batch* p, void* d_a, void* d_b, int32_t* d_piv, int32_t* d_info) {
+  LUHOT_NVTX_FN();
   if (!p) return LUHOT_ERR_INVALID_ARG;
   luhot_ctx* ctx = p->ctx;
   CtxGuard g(ctx);
@@ -533,6 +535,7 @@ int luhot_batch_solve(luhot_batch* p, void* d_a, void* d_b, int32_t* d_piv, int3
 // 32) per size bucket on up to 48 sample systems of that bucket, copied from
 // the caller's data into scratch before each run, and keep the fastest.
 int luhot_batch_autotune(luhot_batch* p, const void* d_a, const void* d_b) {
+  LUHOT_NVTX_FN();
   if (!p) return LUHOT_ERR_INVALID_ARG;
   luhot_ctx* ctx = p->ctx;
   CtxGuard g(ctx);
@@ -648,6 +651,7 @@ int luhot_batch_autotune(luhot_batch* p, const void* d_a, const void* d_b) {
 
 // Host-buffer form: packed host arrays in the plan's layout, staged in and out.
 int luhot_batch_solve_host(luhot_batch* p, void* a, void* b, int32_t* piv, int32_t* info) {
+  LUHOT_NVTX_FN();
   if (!p) return LUHOT_ERR_INVALID_ARG;
   luhot_ctx* ctx = p->ctx;
   if (p->count == 0) return LUHOT_OK;

@@ -177,6 +177,7 @@ extern "C" {
 
 int luhot_dfactor_create(luhot_ctx* ctx, int64_t m, int64_t n, const double* a, int64_t rs, int64_t cs, int mode,
                          uint64_t* piv, int64_t* singular, luhot_factor** out) {
+  LUHOT_NVTX_FN();
   if (!ctx) return LUHOT_ERR_INVALID_ARG;
   CtxGuard g(ctx);
   return factor_create<double>(ctx, m, n, a, rs, cs, nullptr, 0, mode, piv, singular, out);
@@ -184,6 +185,7 @@ int luhot_dfactor_create(luhot_ctx* ctx, int64_t m, int64_t n, const double* a, 
 
 int luhot_sfactor_create(luhot_ctx* ctx, int64_t m, int64_t n, const float* a, int64_t rs, int64_t cs, int mode,
                          uint64_t* piv, int64_t* singular, luhot_factor** out) {
+  LUHOT_NVTX_FN();
   if (!ctx) return LUHOT_ERR_INVALID_ARG;
   CtxGuard g(ctx);
   return factor_create<float>(ctx, m, n, a, rs, cs, nullptr, 0, mode, piv, singular, out);
@@ -191,6 +193,7 @@ int luhot_sfactor_create(luhot_ctx* ctx, int64_t m, int64_t n, const float* a, i
 
 int luhot_dfactor_create_dev(luhot_ctx* ctx, int64_t m, int64_t n, const double* d_a, int64_t lda, int mode,
                              uint64_t* piv, int64_t* singular, luhot_factor** out) {
+  LUHOT_NVTX_FN();
   if (!ctx) return LUHOT_ERR_INVALID_ARG;
   CtxGuard g(ctx);
   if (m * n > 0 && !d_a) return set_error(ctx, LUHOT_ERR_INVALID_ARG, "factor: null pointer");
@@ -199,6 +202,7 @@ int luhot_dfactor_create_dev(luhot_ctx* ctx, int64_t m, int64_t n, const double*
 
 int luhot_dfactor_solve(luhot_factor* f, int64_t nrhs, const double* b, int64_t b_rs, int64_t b_cs, double* x,
                         int64_t x_rs, int64_t x_cs, int trans) {
+  LUHOT_NVTX_FN();
   if (!f) return LUHOT_ERR_INVALID_ARG;
   CtxGuard g(f->ctx);
   int rc = factor_check<double>(f);
@@ -208,6 +212,7 @@ int luhot_dfactor_solve(luhot_factor* f, int64_t nrhs, const double* b, int64_t 
 
 int luhot_sfactor_solve(luhot_factor* f, int64_t nrhs, const float* b, int64_t b_rs, int64_t b_cs, float* x,
                         int64_t x_rs, int64_t x_cs, int trans) {
+  LUHOT_NVTX_FN();
   if (!f) return LUHOT_ERR_INVALID_ARG;
   CtxGuard g(f->ctx);
   int rc = factor_check<float>(f);
@@ -216,6 +221,7 @@ int luhot_sfactor_solve(luhot_factor* f, int64_t nrhs, const float* b, int64_t b
 }
 
 int luhot_dfactor_solve_dev(luhot_factor* f, int64_t nrhs, double* d_b, int64_t ldb, int trans) {
+  LUHOT_NVTX_FN();
   if (!f) return LUHOT_ERR_INVALID_ARG;
   CtxGuard g(f->ctx);
   int rc = factor_check<double>(f);
@@ -226,6 +232,7 @@ int luhot_dfactor_solve_dev(luhot_factor* f, int64_t nrhs, double* d_b, int64_t 
 }
 
 int luhot_factor_read(luhot_factor* f, void* a, int64_t rs, int64_t cs) {
+  LUHOT_NVTX_FN();
   if (!f) return LUHOT_ERR_INVALID_ARG;
   CtxGuard g(f->ctx);
   if (f->m * f->n == 0) return LUHOT_OK;

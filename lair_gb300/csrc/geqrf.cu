@@ -467,18 +467,21 @@ using namespace luhot;
 extern "C" {
 
 int luhot_dgeqrf(luhot_ctx* ctx, int64_t m, int64_t n, double* a, int64_t rs, int64_t cs, double* tau, int mode) {
+  LUHOT_NVTX_FN();
   if (!ctx) return LUHOT_ERR_INVALID_ARG;
   CtxGuard g(ctx);
   return geqrf_host<double>(ctx, m, n, a, rs, cs, tau, mode);
 }
 
 int luhot_sgeqrf(luhot_ctx* ctx, int64_t m, int64_t n, float* a, int64_t rs, int64_t cs, float* tau, int mode) {
+  LUHOT_NVTX_FN();
   if (!ctx) return LUHOT_ERR_INVALID_ARG;
   CtxGuard g(ctx);
   return geqrf_host<float>(ctx, m, n, a, rs, cs, tau, mode);
 }
 
 int luhot_dgeqrf_dev(luhot_ctx* ctx, int64_t m, int64_t n, double* d_a, int64_t lda, double* d_tau, int mode) {
+  LUHOT_NVTX_FN();
   if (!ctx) return LUHOT_ERR_INVALID_ARG;
   CtxGuard g(ctx);
   if (m >= INT32_MAX || n >= INT32_MAX) return set_error(ctx, LUHOT_ERR_INVALID_ARG, "geqrf: invalid dimensions");
@@ -487,6 +490,7 @@ int luhot_dgeqrf_dev(luhot_ctx* ctx, int64_t m, int64_t n, double* d_a, int64_t 
 
 int luhot_dqr_q(luhot_ctx* ctx, int64_t m, int64_t n, const double* qr, int64_t rs, int64_t cs, const double* tau,
                 double* q, int64_t q_rs, int64_t q_cs, int mode) {
+  LUHOT_NVTX_FN();
   if (!ctx) return LUHOT_ERR_INVALID_ARG;
   CtxGuard g(ctx);
   return qr_q_host<double>(ctx, m, n, qr, rs, cs, tau, q, q_rs, q_cs, mode);
@@ -494,6 +498,7 @@ int luhot_dqr_q(luhot_ctx* ctx, int64_t m, int64_t n, const double* qr, int64_t 
 
 int luhot_sqr_q(luhot_ctx* ctx, int64_t m, int64_t n, const float* qr, int64_t rs, int64_t cs, const float* tau,
                 float* q, int64_t q_rs, int64_t q_cs, int mode) {
+  LUHOT_NVTX_FN();
   if (!ctx) return LUHOT_ERR_INVALID_ARG;
   CtxGuard g(ctx);
   return qr_q_host<float>(ctx, m, n, qr, rs, cs, tau, q, q_rs, q_cs, mode);

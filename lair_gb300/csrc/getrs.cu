@@ -481,6 +481,7 @@ cudaError_t trsv_noalloc(const T* a, int64_t lda, T* x, int64_t ldx, int n, int 
 extern "C" int luhot_dgetrs_dev_noalloc(int64_t n, int64_t nrhs, const double* d_lu, int64_t lda,
                                         const int32_t* d_piv, double* d_b, int64_t ldb, int trans,
                                         int mode, void* cuda_stream) {
+  LUHOT_NVTX_FN();
   using namespace luhot;
   if (n < 0 || nrhs < 0 || n >= INT32_MAX || nrhs >= INT32_MAX) return LUHOT_ERR_INVALID_ARG;
   if (mode != LUHOT_MODE_FAST && mode != LUHOT_MODE_EXACT) return LUHOT_ERR_INVALID_ARG;

@@ -600,13 +600,19 @@ int gesv_ir_device(luhot_ctx* ctx, int n, int nrhs, const double* a, int64_t lda
     }
   } guard{e0, e1, e2};
   cudaEventRecord(e0, ctx->stream);
-  rc = ir_factor(s, precision, info);
+  {
+    NvtxRange range("luhot ir: low-precision factorization");
+    rc = ir_factor(s, precision, info);
+  }
   if (rc) return rc;
   cudaEventRecord(e1, ctx->stream);
   for (int c = 0; c < nrhs; ++c) {
     rc = copy_2d(ctx, bc, sizeof(double), b + c, ldb * sizeof(double), sizeof(double), n, cudaMemcpyDeviceToDevice);
     if (rc) return rc;
-    rc = ir_refine(s, bc, xc, solver, tol, max_iter, info);
+    {
+      NvtxRange range("luhot ir: refinement");
+      rc = ir_refine(s, bc, xc, solver, tol, max_iter, info);
+    }
     if (rc) return rc;
     rc = copy_2d(ctx, x + c, ldx * sizeof(double), xc, sizeof(double), sizeof(double), n, cudaMemcpyDeviceToDevice);
     if (rc) return rc;

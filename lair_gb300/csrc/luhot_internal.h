@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 
 #include <atomic>
@@ -169,6 +170,16 @@ struct HostPin {
   luhot_ctx* ctx = nullptr;
   void* p = nullptr;
 };
+
+// NVTX range named after the enclosing C entry point (or a phase), shown on
+// Nsight Systems / Compute timelines; NVTX is a no-op unless a tool attaches.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
+#define LUHOT_NVTX_FN() ::luhot::NvtxRange luhot_nvtx_fn_(__func__)
 
 // Held by every C entry point: serialises calls on a context, makes its
 // device current and clears the last error message.
