@@ -141,6 +141,13 @@ __device__ __forceinline__ int key_reduce_redux(unsigned long long& k, int& i, i
 // fence or counter orders the writers and readers: each 8-byte word is
 // written and read whole.  Tags are step + 1 and the slots are zeroed before
 // each factorization, so a stale word never carries a live tag.
+// Reuse: the slots alternate by step parity, and a CTA rewrites its slot of
+// parity j & 1 at step j + 2 only after it has seen every CTA's step j + 1
+// header.  Each CTA publishes that header only after all its reads of step j
+// have returned their values (the poll consumes them; the segment copy is
+// waited for and its tags checked).  So no read of step j can observe a
+// step j + 2 word; the order comes from the data dependencies, not from a
+// fence.
 __device__ __forceinline__ unsigned long long ld_word(const unsigned long long* p) {
   unsigned long long v;
   asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");

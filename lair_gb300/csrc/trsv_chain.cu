@@ -18,8 +18,11 @@
 // it needs with 32-byte loads (lane L takes columns 4L..4L+3 of the block,
 // the columns its float4 loads of the factor cover) and accepts them when
 // every tag is this launch's epoch; the epoch grows per launch, so words of
-// an earlier sweep are never taken.  Every wait is bounded by the context's
-// wait limit and reports LUHOT_ERR_TIMEOUT on expiry.
+// an earlier sweep are never taken.  Within a launch every word is written
+// once (by the CTA of its block), and launches on the context's stream do
+// not overlap, so no word is rewritten while a reader may still want it.
+// Every wait is bounded by the context's wait limit and reports
+// LUHOT_ERR_TIMEOUT on expiry.
 //
 // Layout of the work: 16 warps x 8 rows; lane L holds per-row partial sums
 // over its 4 columns of every tile, reduced once at the end with a 9-shuffle
