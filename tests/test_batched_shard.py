@@ -82,3 +82,36 @@ def test_two_gloo_ranks_solve_disjoint_shards():
     assert b0 == 0 and e0 == b1 and e1 == 64
     assert s0 == s1
     assert s0[5] == 4 and all(v == -1 for i, v in enumerate(s0) if i != 5)
+
+
+def test_pack_unpack_round_trip_and_layout():
+    # Packed layout of the batched ABI: A_i row-major back to back, b_i (and
+    # the pivots) back to back, offsets the running sums of n_i^2 and n_i.
+    rng = np.random.default_rng(5)
+    sizes = [1, 3, 8, 2]
+    mats = [rng.standard_normal((n, n)) for n in sizes]
+    rhs = [rng.standard_normal(n) for n in sizes]
+    a, b = batched.pack([np.asfortranarray(m) for m in mats], rhs, dtype=np.float32)
+    assert a.dtype == np.float32 and a.size == sum(n * n for n in sizes) and b.size == sum(sizes)
+    piv = np.arange(b.size, dtype=np.int32)
+    off = 0
+    for (ai, bi, pi), m, v, n in zip(batched.unpack(sizes, a, b, piv), mats, rhs, sizes):
+        assert np.array_equal(ai, m.astype(np.float32)) and np.array_equal(bi, v.astype(np.float32))
+        assert np.array_equal(pi, np.arange(off, off + n))
+        off += n
+    empty_a, empty_b = batched.pack([], [])
+    assert empty_a.size == 0 and empty_b.size == 0
+
+
+def test_synthetic_batch_is_the_benchmark_distribution():
+    sizes, a, b = batched.synthetic_batch(500, seed=7, nmin=8, nmax=256)
+    assert sizes.min() >= 8 and sizes.max() <= 256 and a.size == int(np.sum(sizes.astype(np.int64) ** 2))
+    again = batched.synthetic_batch(500, seed=7, nmin=8, nmax=256)
+    assert all(np.array_equal(x, y) for x, y in zip((sizes, a, b), again))  # seeded
+    # about half the systems carry the + n I shift (their diagonal dominates)
+    ao, shifted = 0, 0
+    for n in sizes:
+        d = a[ao:ao + n * n].reshape(n, n).diagonal()
+        shifted += int(np.all(d >= n - 1))
+        ao += int(n) * int(n)
+    assert 0.4 * len(sizes) < shifted < 0.6 * len(sizes)
