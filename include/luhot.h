@@ -297,11 +297,16 @@ int luhot_sqr_q(luhot_ctx* ctx, int64_t m, int64_t n, const float* qr, int64_t r
  * keeps until exit.  The caller passes factors, pivots and B (overwritten by
  * X) in device memory and the stream to run on (NULL = legacy default).
  * Limit: 4*n rounded up to 256 bytes plus 8*n*nrhs bytes must fit in the
- * scratch, else LUHOT_ERR_UNSUPPORTED.  The first call on each device looks up
- * the array's device address (cudaGetSymbolAddress), so make that first call
- * before any stream capture.  All calls share the array: calls that overlap
- * on the GPU race on it.  Results equal luhot_dgetrs_dev's.  No counterpart
- * in lair (lair's getrs allocates its result on the host). */
+ * scratch, else LUHOT_ERR_UNSUPPORTED (e.g. n = 1024 takes up to 511
+ * right-hand sides); nothing else limits nrhs.  The first call on each device
+ * looks up the array's device address (cudaGetSymbolAddress), so make that
+ * first call before any stream capture; the lookup runs again after the
+ * device's context changes (after a cudaDeviceReset), so make the first call
+ * after a reset outside any capture too.  All calls share the array: calls
+ * that overlap on the GPU race on it.  Exact mode without trans gives the
+ * bits of luhot_dgetrs_dev (lair's order); fast mode and trans agree with it
+ * to fast-mode rounding (the sweeps group the sums differently).  No
+ * counterpart in lair (lair's getrs allocates its result on the host). */
 int luhot_dgetrs_dev_noalloc(int64_t n, int64_t nrhs, const double* d_lu, int64_t lda,
                              const int32_t* d_piv, double* d_b, int64_t ldb, int trans, int mode,
                              void* cuda_stream);

@@ -8,7 +8,10 @@
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <new>
+#include <set>
+#include <utility>
 #include <vector>
 
 #include "common.cuh"
@@ -19,6 +22,26 @@ namespace luhot {
 int set_error(luhot_ctx* ctx, int status, const std::string& msg) {
   if (ctx) ctx->last_error = msg;
   return status;
+}
+
+cudaError_t allow_max_dynamic_smem(const void* kernel) {
+  static std::mutex mu;
+  static std::set<std::pair<const void*, int>> raised;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lock(mu);
+  if (raised.count({kernel, dev})) return cudaSuccess;
+  int optin = 0;
+  e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e != cudaSuccess) return e;
+  cudaFuncAttributes fa;
+  e = cudaFuncGetAttributes(&fa, kernel);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
+  if (e != cudaSuccess) return e;
+  raised.insert({kernel, dev});
+  return cudaSuccess;
 }
 
 int ensure_buf(luhot_ctx* ctx, DevBuf& b, size_t bytes) {
@@ -244,28 +267,64 @@ template int stage_out<double>(luhot_ctx*, const double*, int64_t, double*, int6
 template int stage_out<float>(luhot_ctx*, const float*, int64_t, float*, int64_t, int64_t, int64_t, int64_t, DevBuf&);
 template int launch_transpose<double>(luhot_ctx*, const double*, int64_t, double*, int64_t, int, int);
 
+namespace {
+// Host ranges this library page-locked, keyed by start address, with the
+// number of calls currently using each.  cudaHostRegister refuses
+// overlapping ranges, so the ranges are disjoint.
+struct PinnedRange {
+  uintptr_t end;
+  int users;
+};
+std::mutex g_pin_mu;
+std::map<uintptr_t, PinnedRange> g_pinned;
+}  // namespace
+
 HostPin::HostPin(luhot_ctx* c, const void* base, int64_t m, int64_t n, int64_t rs, int64_t cs, size_t elem)
     : ctx(c) {
   if (!base || m <= 0 || n <= 0 || rs < 0 || cs < 0) return;
   const size_t span = ((size_t)(m - 1) * (size_t)rs + (size_t)(n - 1) * (size_t)cs + 1) * elem;
   if (span < (size_t)8 << 20) return;
+  const uintptr_t lo = reinterpret_cast<uintptr_t>(base), hi = lo + span;
+  std::lock_guard<std::mutex> lock(g_pin_mu);
+  // A call on another context may have pinned this array (or part of it):
+  // hold those ranges for this call instead of registering again, so that
+  // the other call's release cannot unpin them under this call's copies.
+  auto it = g_pinned.upper_bound(lo);
+  if (it != g_pinned.begin()) --it;
+  for (; it != g_pinned.end() && it->first < hi; ++it) {
+    if (it->second.end > lo) {
+      ++it->second.users;
+      held.push_back(it->first);
+    }
+  }
+  if (!held.empty()) return;
   cudaPointerAttributes at;
   if (cudaPointerGetAttributes(&at, base) != cudaSuccess) {
     cudaGetLastError();
     return;
   }
-  if (at.type != cudaMemoryTypeUnregistered) return;
-  if (cudaHostRegister(const_cast<void*>(base), span, cudaHostRegisterDefault) == cudaSuccess)
-    p = const_cast<void*>(base);
-  else
+  if (at.type != cudaMemoryTypeUnregistered) return;  // the caller's own pinned or managed memory
+  if (cudaHostRegister(const_cast<void*>(base), span, cudaHostRegisterDefault) == cudaSuccess) {
+    g_pinned[lo] = PinnedRange{hi, 1};
+    held.push_back(lo);
+  } else {
     cudaGetLastError();
+  }
 }
 
 HostPin::~HostPin() {
-  if (!p) return;
-  cudaStreamSynchronize(ctx->stream);
-  cudaHostUnregister(p);
-  cudaGetLastError();
+  if (held.empty()) return;
+  cudaStreamSynchronize(ctx->stream);  // this call's copies from the range are done
+  std::lock_guard<std::mutex> lock(g_pin_mu);
+  for (uintptr_t key : held) {
+    auto it = g_pinned.find(key);
+    if (it == g_pinned.end()) continue;
+    if (--it->second.users == 0) {
+      cudaHostUnregister(reinterpret_cast<void*>(key));
+      cudaGetLastError();
+      g_pinned.erase(it);
+    }
+  }
 }
 
 static bool dims_ok(int64_t m, int64_t n) {

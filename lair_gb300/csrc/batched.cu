@@ -374,7 +374,7 @@ static int grid_for(luhot_ctx* ctx, int dtype, int mode) {
     k = mode == LUHOT_MODE_EXACT ? (const void*)batched_lu_kernel<double, true> : (const void*)batched_lu_kernel<double, false>;
   else
     k = mode == LUHOT_MODE_EXACT ? (const void*)batched_lu_kernel<float, true> : (const void*)batched_lu_kernel<float, false>;
-  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBatchSmem);
+  allow_max_dynamic_smem(k);
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kBatchThreads, kBatchSmem) != cudaSuccess) {
     cudaGetLastError();
     per_sm = 1;

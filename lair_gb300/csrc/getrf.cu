@@ -1093,8 +1093,7 @@ static int launch_panel(luhot_ctx* ctx, T* a, int64_t lda, int m, int k0, int w,
   if (panel_smem_bytes<T>(rows_per, w) > (size_t)max_smem)
     return set_error(ctx, LUHOT_ERR_UNSUPPORTED, "panel does not fit in shared memory");
   const size_t smem = panel_smem_bytes<T>(rows_per, w);
-  LUHOT_CUDA_TRY(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)smem));
+  LUHOT_CUDA_TRY(ctx, allow_max_dynamic_smem(kern));
   int per_sm = 0;
   LUHOT_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, panel_threads<T>(), smem));
   if (per_sm * ctx->num_sms < P)
@@ -1136,14 +1135,12 @@ static int launch_gemm(luhot_ctx* ctx, T* a, int64_t lda, int r0, int c0, int kk
     const bool aligned = (lda % 2 == 0) && (kk0 % 2 == 0) && (c0 % 2 == 0) &&
                          (reinterpret_cast<uintptr_t>(a) % 16 == 0);
     if (aligned && smem_p <= (size_t)ctx->max_smem_optin) {
-      LUHOT_CUDA_TRY(ctx, cudaFuncSetAttribute(gemm_dmma_persistent_kernel,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_p));
+      LUHOT_CUDA_TRY(ctx, allow_max_dynamic_smem(gemm_dmma_persistent_kernel));
       prof_begin(ctx, kProfGemm);
       gemm_dmma_persistent_kernel<<<std::min(tiles, ctx->num_sms), 256, smem_p, stream>>>(a, lda, r0, c0, kk0, K,
                                                                                           M, N);
     } else {
-      LUHOT_CUDA_TRY(ctx, cudaFuncSetAttribute(gemm_dmma_kernel,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      LUHOT_CUDA_TRY(ctx, allow_max_dynamic_smem(gemm_dmma_kernel));
       dim3 grid((N + kDmmaBN - 1) / kDmmaBN, (M + kDmmaBM - 1) / kDmmaBM);
       prof_begin(ctx, kProfGemm);
       gemm_dmma_kernel<<<grid, 256, smem, stream>>>(a, lda, r0, c0, kk0, K, M, N);
@@ -1178,8 +1175,7 @@ static int getrf_impl(luhot_ctx* ctx, int m, int n, T* a, int64_t lda, int* piv,
       prof_begin(ctx, kProfLaswp);
       int* moves = reinterpret_cast<int*>(static_cast<char*>(ctx->panel_scratch) + kPanelSlotBytes);
       const size_t lsm = (size_t)2 * w * 32 * sizeof(T);
-      LUHOT_CUDA_TRY(ctx, cudaFuncSetAttribute(laswp_moves_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               (int)lsm));
+      LUHOT_CUDA_TRY(ctx, allow_max_dynamic_smem(laswp_moves_kernel<T>));
       laswp_moves_kernel<T><<<(ncols_swap + 31) / 32, dim3(32, 8), lsm, stream>>>(
           a, lda, moves, moves + 4 * kMaxPanelWidth, 2 * w, k0, c_right, n);
       prof_end(ctx, kProfLaswp, 0.0, 4.0 * w * ncols_swap * sizeof(T));
@@ -1190,21 +1186,18 @@ static int getrf_impl(luhot_ctx* ctx, int m, int n, T* a, int64_t lda, int* piv,
       prof_begin(ctx, kProfTrsm);
       if (!kExact && w <= 64) {
         const size_t smem = ((size_t)64 * 64 + (size_t)64 * kTrsmCols) * sizeof(T);
-        LUHOT_CUDA_TRY(ctx, cudaFuncSetAttribute(trsm_fast_kernel<T, 64>,
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        LUHOT_CUDA_TRY(ctx, allow_max_dynamic_smem(trsm_fast_kernel<T, 64>));
         trsm_fast_kernel<T, 64><<<tgrid, kTrsmCols, smem, stream>>>(a, lda, k0, w, c_right, n);
       } else if (!kExact && std::is_same<T, float>::value && w <= 128) {
         if constexpr (std::is_same<T, float>::value) {
           const size_t smem = ((size_t)128 * 128 + (size_t)128 * kTrsmCols) * sizeof(T);
-          LUHOT_CUDA_TRY(ctx, cudaFuncSetAttribute(trsm_fast_kernel<T, 128>,
-                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+          LUHOT_CUDA_TRY(ctx, allow_max_dynamic_smem(trsm_fast_kernel<T, 128>));
           trsm_fast_kernel<T, 128><<<tgrid, kTrsmCols, smem, stream>>>(a, lda, k0, w, c_right, n);
         }
       } else {
         const size_t smem = ((size_t)w * w + (size_t)w * kTrsmCols) * sizeof(T);
         auto kern = trsm_kernel<T, kExact>;
-        LUHOT_CUDA_TRY(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)smem));
+        LUHOT_CUDA_TRY(ctx, allow_max_dynamic_smem(kern));
         kern<<<tgrid, kTrsmCols, smem, stream>>>(a, lda, k0, w, c_right, n);
       }
       prof_end(ctx, kProfTrsm, (double)w * (w - 1) * (n - c_right),

@@ -274,8 +274,7 @@ int getrf_colmajor_host(luhot_ctx* ctx, int64_t m, int64_t n, T* a, int64_t rs, 
   rc = reset_status(ctx);
   if (rc) return rc;
   const size_t smem = (size_t)5 * m * sizeof(T);
-  LUHOT_CUDA_TRY(ctx, cudaFuncSetAttribute(getrf_colmajor_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)smem));
+  LUHOT_CUDA_TRY(ctx, allow_max_dynamic_smem(getrf_colmajor_kernel<T>));
   prof_begin(ctx, kProfPanel);
   getrf_colmajor_kernel<T><<<1, kCmThreads, smem, ctx->stream>>>(d_a, ld, (int)m, (int)n, d_piv, ctx->d_status);
   prof_end(ctx, kProfPanel, 2.0 / 3.0 * (double)k * k * k, 2.0 * m * n * sizeof(T));

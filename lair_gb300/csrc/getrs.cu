@@ -22,7 +22,10 @@
 // blocked kernels below (a diagonal-block kernel, sequential per right-hand
 // side, and an update kernel for the rows outside the block), which need no
 // scratch besides the permutation and the right-hand-side copy.
+#include <cuda.h>
+
 #include <algorithm>
+#include <mutex>
 
 #include "common.cuh"
 #include "luhot_internal.h"
@@ -211,7 +214,7 @@ int getrs_perm(luhot_ctx* ctx, const int* piv, int n, int* perm) {
   const size_t bytes = 2 * (size_t)n * sizeof(int);  // permutation + pivots
   const int use_smem = bytes <= (size_t)ctx->max_smem_optin ? 1 : 0;
   const size_t smem = use_smem ? bytes : 0;
-  LUHOT_CUDA_TRY(ctx, cudaFuncSetAttribute(perm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  LUHOT_CUDA_TRY(ctx, allow_max_dynamic_smem(perm_kernel));
   prof_begin(ctx, kProfPermute);
   perm_kernel<<<1, 1024, smem, ctx->stream>>>(piv, n, perm, use_smem);
   prof_end(ctx, kProfPermute, 0.0, 2.0 * n * sizeof(int));
@@ -300,9 +303,7 @@ int getrs_apply(luhot_ctx* ctx, int n, int nrhs, const T* lu, int64_t lda, const
     if (exact) {
       const size_t xs = (size_t)n * sizeof(T);
       const int use_smem = xs <= (size_t)ctx->max_smem_optin - 1024 ? 1 : 0;
-      LUHOT_CUDA_TRY(ctx, cudaFuncSetAttribute(back_exact_kernel<T>,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               use_smem ? (int)xs : 0));
+      LUHOT_CUDA_TRY(ctx, allow_max_dynamic_smem(back_exact_kernel<T>));
       prof_begin(ctx, kProfTrsv);
       back_exact_kernel<T><<<nrhs, 32, use_smem ? xs : 0, stream>>>(lu, lda, w, ldw, n, use_smem);
       prof_end(ctx, kProfTrsv, (double)n * n * nrhs, ((double)n * n / 2 + 2.0 * total) * sizeof(T));
@@ -416,12 +417,46 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 namespace {
 constexpr int kNoAllocMaxDevices = 64;
 std::mutex g_noalloc_mu;
-void* g_noalloc_addr[kNoAllocMaxDevices] = {};  // device address of g_noalloc_scratch, per device
+void* g_noalloc_addr[kNoAllocMaxDevices] = {};            // device address of g_noalloc_scratch, per device
+unsigned long long g_noalloc_ctx[kNoAllocMaxDevices] = {};  // id of the context that address belongs to
 int g_noalloc_smem[kNoAllocMaxDevices] = {};
 
-// Once per device, with that device current: look up the device address of
-// the scratch array.  In host code `g_noalloc_scratch` names a host-side
-// stand-in, never the device memory, so kernels only ever get this address.
+// Unique id of the calling thread's current CUDA context (cuCtxGetId, reached
+// through the runtime's driver entry points), 0 when there is none or the
+// driver cannot tell.  A context made after a cudaDeviceReset has a new id.
+unsigned long long current_context_id() {
+  using GetCurrent = CUresult (*)(CUcontext*);
+  using GetId = CUresult (*)(CUcontext, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<GetCurrent>(p);
+    p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<GetId>(p);
+    cudaGetLastError();
+  });
+  if (!get_current || !get_id) return 0;
+  CUcontext c = nullptr;
+  unsigned long long id = 0;
+  if (get_current(&c) != CUDA_SUCCESS || !c) return 0;
+  if (get_id(c, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
+
+// Set-up, once per device with that device current: look up the device
+// address of the scratch array.  In host code `g_noalloc_scratch` names a
+// host-side stand-in, never the device memory, so kernels only ever get this
+// address.  The address belongs to the device's context: when the context
+// changes (a cudaDeviceReset ends it, the next call gets a new one), the
+// set-up runs again, so no call launches with an address of a context that
+// is gone.
 int noalloc_setup(void** scratch, int* max_smem) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) {
@@ -430,7 +465,8 @@ int noalloc_setup(void** scratch, int* max_smem) {
   }
   if (dev < 0 || dev >= kNoAllocMaxDevices) return LUHOT_ERR_UNSUPPORTED;
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_addr[dev]) {
+  const unsigned long long ctx_id = current_context_id();
+  if (!g_noalloc_addr[dev] || ctx_id == 0 || ctx_id != g_noalloc_ctx[dev]) {
     void* p = nullptr;
     if (cudaGetSymbolAddress((void**)&p, g_noalloc_scratch) != cudaSuccess || !p) {
       cudaGetLastError();
@@ -443,21 +479,25 @@ int noalloc_setup(void** scratch, int* max_smem) {
     }
     g_noalloc_smem[dev] = smem;
     g_noalloc_addr[dev] = p;
+    g_noalloc_ctx[dev] = current_context_id();  // the lookup made the context current if none was
   }
   *scratch = g_noalloc_addr[dev];
   *max_smem = g_noalloc_smem[dev];
   return LUHOT_OK;
 }
 
+// Right-hand sides per update launch: the update kernel stages its block of
+// x (64 rows x chunk) in shared memory.
+constexpr int kNoAllocRhsChunk = 256;
+
 template <typename T, bool kExact, bool kLower, bool kUnit, bool kTrans>
 cudaError_t trsv_noalloc(const T* a, int64_t lda, T* x, int64_t ldx, int n, int nrhs, cudaStream_t stream) {
   const int bsz = kTrsvBlock;
   auto dk = trsv_diag_kernel<T, kExact, kLower, kUnit, kTrans>;
   auto uk = trsv_update_kernel<T, kExact, kTrans>;
-  cudaError_t e = cudaFuncSetAttribute(dk, cudaFuncAttributeMaxDynamicSharedMemorySize, bsz * bsz * (int)sizeof(T));
+  cudaError_t e = allow_max_dynamic_smem(dk);
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(uk, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)(((size_t)64 * (bsz + 1) + (size_t)bsz * nrhs) * sizeof(T)));
+  e = allow_max_dynamic_smem(uk);
   if (e != cudaSuccess) return e;
   const int nblk = (n + bsz - 1) / bsz;
   for (int s = 0; s < nblk; ++s) {
@@ -467,9 +507,10 @@ cudaError_t trsv_noalloc(const T* a, int64_t lda, T* x, int64_t ldx, int n, int 
     dk<<<1, 128, (size_t)bs * bs * sizeof(T), stream>>>(a, lda, x, ldx, j0, bs, nrhs);
     const int i_begin = kLower ? j0 + bs : 0;
     const int i_end = kLower ? n : j0;
-    if (i_end > i_begin) {
-      const size_t sm = ((size_t)64 * (bs + 1) + (size_t)bs * nrhs) * sizeof(T);
-      uk<<<(i_end - i_begin + 63) / 64, 256, sm, stream>>>(a, lda, x, ldx, j0, bs, i_begin, i_end, nrhs);
+    for (int c0 = 0; i_end > i_begin && c0 < nrhs; c0 += kNoAllocRhsChunk) {
+      const int nc = std::min(kNoAllocRhsChunk, nrhs - c0);
+      const size_t sm = ((size_t)64 * (bs + 1) + (size_t)bs * nc) * sizeof(T);
+      uk<<<(i_end - i_begin + 63) / 64, 256, sm, stream>>>(a, lda, x + c0, ldx, j0, bs, i_begin, i_end, nc);
     }
   }
   return cudaGetLastError();
@@ -494,8 +535,6 @@ extern "C" int luhot_dgetrs_dev_noalloc(int64_t n, int64_t nrhs, const double* d
   int max_smem = 0;
   int rc = noalloc_setup(&scratch, &max_smem);
   if (rc) return rc;
-  if (((size_t)64 * (kTrsvBlock + 1) + (size_t)kTrsvBlock * nrhs) * sizeof(double) > (size_t)max_smem)
-    return LUHOT_ERR_UNSUPPORTED;
   cudaStream_t stream = static_cast<cudaStream_t>(cuda_stream);
   int* perm = static_cast<int*>(scratch);
   double* w = reinterpret_cast<double*>(static_cast<unsigned char*>(scratch) + perm_bytes);
@@ -504,8 +543,7 @@ extern "C" int luhot_dgetrs_dev_noalloc(int64_t n, int64_t nrhs, const double* d
   const int64_t total = n * nrhs;
   const int pblocks = (int)((total + 255) / 256);
   const int use_smem = 2 * (size_t)n * sizeof(int) <= (size_t)max_smem ? 1 : 0;
-  if (cudaFuncSetAttribute(perm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           use_smem ? (int)(2 * n * sizeof(int)) : 0) != cudaSuccess) {
+  if (allow_max_dynamic_smem(perm_kernel) != cudaSuccess) {
     cudaGetLastError();
     return LUHOT_ERR_CUDA;
   }
@@ -517,9 +555,7 @@ extern "C" int luhot_dgetrs_dev_noalloc(int64_t n, int64_t nrhs, const double* d
       e = trsv_noalloc<double, true, true, true, false>(d_lu, lda, w, ldw, nn, nr, stream);
       const size_t xs = (size_t)n * sizeof(double);
       const int xs_smem = xs <= (size_t)max_smem - 1024 ? 1 : 0;
-      if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(back_exact_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 xs_smem ? (int)xs : 0);
+      if (e == cudaSuccess) e = allow_max_dynamic_smem(back_exact_kernel<double>);
       if (e == cudaSuccess)
         back_exact_kernel<double><<<nr, 32, xs_smem ? xs : 0, stream>>>(d_lu, lda, w, ldw, nn, xs_smem);
     } else {

@@ -159,16 +159,20 @@ template <typename T, typename TA = T>
 int invert_diag_blocks(luhot_ctx* ctx, int n, const TA* lu, int64_t lda, T* dinv_l, T* dinv_u);
 
 // Page-locks a caller's host array for the duration of one call (large
-// arrays only, if not already registered), so its copies run as DMA at the
-// host link's full rate whatever the state of the pageable memory; the stream
-// is synchronised before the pages are released.  Strides in elements.
+// arrays only), so its copies run as DMA at the host link's full rate
+// whatever the state of the pageable memory; the stream is synchronised
+// before the pages are released.  Ranges this library pinned carry a
+// process-wide count of the calls using them (calls on other contexts and
+// threads may pass the same array), and a range is unpinned only when its
+// last user ends.  Memory the caller registered itself is left alone.
+// Strides in elements.
 struct HostPin {
   HostPin(luhot_ctx* ctx, const void* base, int64_t m, int64_t n, int64_t rs, int64_t cs, size_t elem);
   ~HostPin();
   HostPin(const HostPin&) = delete;
   HostPin& operator=(const HostPin&) = delete;
   luhot_ctx* ctx = nullptr;
-  void* p = nullptr;
+  std::vector<uintptr_t> held;  // start addresses of the pinned ranges this call uses
 };
 
 // NVTX range named after the enclosing C entry point (or a phase), shown on
@@ -201,6 +205,18 @@ int stage_out(luhot_ctx* ctx, const T* d, int64_t ldd, T* h, int64_t m, int64_t 
 // dst (row-major, ldd) <- transpose of src (rows x cols, lds).
 template <typename T>
 int launch_transpose(luhot_ctx* ctx, const T* src, int64_t lds, T* dst, int64_t ldd, int rows, int cols);
+
+// Lets launches of `kernel` on the current device request up to the device's
+// opt-in shared-memory limit (less the kernel's static shared memory).  The
+// attribute is per kernel and device for the whole process, so it is set
+// once, under a process-wide lock, and never lowered: a launch on one thread
+// can never find the limit lowered by a call on another thread between its
+// check and its launch.  Launches still pass their own dynamic size.
+cudaError_t allow_max_dynamic_smem(const void* kernel);
+template <typename K>
+cudaError_t allow_max_dynamic_smem(K* kernel) {
+  return allow_max_dynamic_smem(reinterpret_cast<const void*>(kernel));
+}
 
 inline void count_launch(luhot_ctx* ctx, int64_t k = 1) { ctx->launches.fetch_add(k); }
 

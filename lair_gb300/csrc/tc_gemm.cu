@@ -801,8 +801,7 @@ static int launch_tc(luhot_ctx* ctx, float* a, int64_t lda, int k0, int w, int m
     rc = make_c_map(ctx, &tC, cbase, M, N, lda);
     if (rc) return rc;
     auto kern = tc_gemm_persistent_kernel<KIND>;
-    LUHOT_CUDA_TRY(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)TcShape<KIND>::kSmem));
+    LUHOT_CUDA_TRY(ctx, allow_max_dynamic_smem(kern));
     const int tiles = ((M + 127) / 128) * ((N + 127) / 128);
     prof_begin(ctx, kProfGemm);
     kern<<<std::min(tiles, ctx->num_sms), kTcThreads, TcShape<KIND>::kSmem, stream>>>(tA, tB, tC, M, N, kalloc,
@@ -811,7 +810,7 @@ static int launch_tc(luhot_ctx* ctx, float* a, int64_t lda, int k0, int w, int m
     const int kbox = KIND == kTcTF32 ? 32 : 64;
     const size_t smem = KIND == kTcBF16x3 ? 1024 + 6 * 16384 : 1024 + (size_t)(kalloc / kbox) * 2 * 16384;
     auto kern = KIND == kTcBF16x3 ? tc_gemm_x3_kernel : tc_gemm_kernel<KIND>;
-    LUHOT_CUDA_TRY(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    LUHOT_CUDA_TRY(ctx, allow_max_dynamic_smem(kern));
     dim3 grid((N + 127) / 128, (M + 127) / 128);
     prof_begin(ctx, kProfGemm);
     kern<<<grid, 128, smem, stream>>>(tA, tB, cbase, lda, M, N, w, scal + 4, ctx->d_status);

@@ -358,7 +358,7 @@ static cudaError_t launch_case(cudaStream_t stream, const TA* a, int64_t lda, T*
 #define LUHOT_TRSV_NR(NR)                                                                       \
   {                                                                                             \
     auto k = trsv_syncfree_kernel<T, TA, EX, LO, UN, TR, NR>;                                   \
-    e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);        \
+    e = allow_max_dynamic_smem(k);                                                              \
     if (e != cudaSuccess) return e;                                                             \
     k<<<nblk, kThreads, smem, stream>>>(a, lda, x, ldx, n, nc, flags, ticket, st, dinv);        \
     return cudaGetLastError();                                                                  \
@@ -451,7 +451,7 @@ cudaError_t launch_trsv_invert_diag(cudaStream_t stream, const TA* a, int64_t ld
   const size_t smem = 2 * (size_t)kBS * kLds * sizeof(T);
   const int nblk = trsv_syncfree_blocks(n);
   auto k = lower ? trsv_invert_diag_kernel<T, TA, true, true> : trsv_invert_diag_kernel<T, TA, false, false>;
-  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = allow_max_dynamic_smem(k);
   if (e != cudaSuccess) return e;
   k<<<nblk, kBS, smem, stream>>>(a, lda, n, dinv);
   return cudaGetLastError();

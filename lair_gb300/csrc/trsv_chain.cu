@@ -314,7 +314,7 @@ cudaError_t launch_trsv_chain_invert(cudaStream_t stream, const float* a, int64_
   if (n <= 0) return cudaSuccess;
   const size_t smem = (size_t)kCB * (kCB + 1) * (sizeof(T) + sizeof(float));
   auto k = lower ? trsv_chain_invert_kernel<T, true> : trsv_chain_invert_kernel<T, false>;
-  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = allow_max_dynamic_smem(k);
   if (e != cudaSuccess) return e;
   k<<<trsv_chain_blocks(n), kCB, smem, stream>>>(a, lda, n, dinv);
   return cudaGetLastError();
@@ -327,7 +327,7 @@ cudaError_t launch_trsv_chain(cudaStream_t stream, const float* a, int64_t lda, 
   if (n <= 0) return cudaSuccess;
   const size_t smem = ((size_t)kCB * kCB + 3 * (size_t)kCB) * sizeof(T);
   auto k = lower ? trsv_chain_kernel<T, true> : trsv_chain_kernel<T, false>;
-  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = allow_max_dynamic_smem(k);
   if (e == cudaSuccess) e = cudaMemsetAsync(ticket, 0, sizeof(int), stream);
   if (e != cudaSuccess) return e;
   k<<<trsv_chain_blocks(n), kCThreads, smem, stream>>>(a, lda, x, n, dinv, xt, epoch, ticket, st);

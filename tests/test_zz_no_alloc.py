@@ -61,6 +61,33 @@ def test_noalloc_matches_existing_entry_point_twice(mode, trans):
         lib.luhot_set_stream(ctx, None)
 
 
+@pytest.mark.parametrize("mode", [_lib.MODE_FAST, _lib.MODE_EXACT])
+def test_noalloc_many_right_hand_sides(mode):
+    """400 right-hand sides of order 64 fit the scratch; the block updates
+    take them 256 at a time, so shared memory sets no smaller limit."""
+    torch = pytest.importorskip("torch")
+    lib, ctx = _lib.load(), _lib.context()
+    n, nrhs = 64, 400
+    _, d_a, d_piv = _factor(torch, lib, ctx, n, 300)
+    b = np.random.default_rng(301).standard_normal((n, nrhs))
+    d_ref = torch.from_numpy(b).cuda().contiguous()
+    d_new = torch.from_numpy(b).cuda().contiguous()
+    torch.cuda.synchronize()
+    _lib.check(lib.luhot_dgetrs_dev(ctx, n, nrhs, d_a.data_ptr(), n, d_piv.data_ptr(), d_ref.data_ptr(), nrhs, 0,
+                                    mode), ctx)
+    torch.cuda.synchronize()
+    for _ in range(2):
+        d_new.copy_(torch.from_numpy(b).cuda())
+        torch.cuda.synchronize()
+        rc = lib.luhot_dgetrs_dev_noalloc(n, nrhs, d_a.data_ptr(), n, d_piv.data_ptr(), d_new.data_ptr(), nrhs, 0,
+                                          mode, None)
+        assert rc == _lib.LUHOT_OK
+        torch.cuda.synchronize()
+        ref, new = d_ref.cpu().numpy(), d_new.cpu().numpy()
+        atol = 0 if mode == _lib.MODE_EXACT else 1e-8 * np.abs(ref).max()
+        np.testing.assert_allclose(new, ref, rtol=0, atol=atol)
+
+
 def test_noalloc_rejects_sizes_beyond_its_scratch():
     torch = pytest.importorskip("torch")
     lib = _lib.load()
