@@ -1,8 +1,9 @@
 """Benchmark: Ax=b GFLOP/s at backward error <= n*eps64 on one GB300.
 
 Workload (default): plain FP64 getrf + getrs, n = 16384, 16 right-hand sides,
-A and B iid N(0, 1) from a seeded Philox generator (synthetic; no dataset
-exists for this metric).  One step = restore A and B in HBM, factor, solve.
+A and B iid N(0, 1) from the seeded portable generator (lair_gb300.synthetic;
+synthetic, no dataset exists for this metric), the inputs of the committed
+lair reference results, so the line carries a parity key.  One step = restore A and B in HBM, factor, solve.
 GFLOP/s = (2/3 n^3 + 2 n^2 nrhs) / time.  The solution's normwise backward
 error ||b - Ax||_inf / (||A||_inf ||x||_inf + ||b||_inf) is checked against
 n * 2^-53 after the timed steps.
@@ -13,7 +14,12 @@ Printed as one JSON line (rank 0):
             (luhot_dgesv: A, B copied in and X copied out every step)
   roofline  the Schur-update GEMM (the dominant kernel) against the FP64
             tensor-core peak measured in this run
-  cpu_baseline  lair's algorithm (the CPU oracle) on a bounded sample
+  parity    pivots, ||PA - LU|| and the solution error against lair's
+            results for the same inputs (tests/golden fixtures)
+  cpu_baseline  lair's algorithm (the CPU oracle) on a bounded sample, plus
+            one complete n = 4096 run and its n^3 extrapolation (labelled)
+  adjoint   the backward solve (lambda = A^-T W, dA, dB) at n = 2048, nrhs = 8
+  batched   10,000 uneven systems, sharded over ranks by work when N > 1
   ir        mixed-precision LU + iterative refinement on the kappa-conditioned
             n = 16384 system, when built
 
@@ -141,18 +147,43 @@ def cpu_sample(n: int, seed: int, elim_steps: int, state=None):
     return fl, (t2 - t0), state
 
 
-def cpu_baseline(n: int, seconds: float = 12.0):
+def cpu_full_run(n: int, nrhs: int):
+    """One complete solve in lair's order on one core: getrf_row_major of an
+    n x n N(0,1) matrix and lair's single-RHS getrs for each of nrhs columns."""
+    import oracle
+    from lair_gb300 import synthetic
+
+    a = synthetic.normal_matrix(10 * n + 1, n, n)
+    b = synthetic.normal_matrix(10 * n + 2, n, nrhs)
+    t0 = time.perf_counter()
+    piv, _ = oracle.getrf_row_major(a)
+    for j in range(nrhs):
+        oracle.getrs(a, piv, np.ascontiguousarray(b[:, j]))
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(n: int, nrhs: int, seconds: float = 12.0, full_n: int = 4096):
     fl_total, t_total, steps, state = 0.0, 0.0, 0, None
     while t_total < seconds and (state is None or state["next"] < n):
         fl, t, state = cpu_sample(n, 1234, 2, state)
         fl_total += fl
         t_total += t
         steps += 1
-    return {"value": fl_total / t_total / 1e9, "unit": "GFLOP/s", "cores": 1, "kind": "port",
-            "sample": (f"lair getrf_row_major + getrs restated in C++ (-O2 -ffp-contract=off), 1 thread: "
-                       f"the first {state['next']} elimination steps of an n={n} N(0,1) matrix plus "
-                       f"{steps} single-RHS getrs at n={n}; {t_total:.1f} s of CPU work"),
-            "host": os.uname().machine, "host_cores_total": os.cpu_count()}
+    out = {"value": fl_total / t_total / 1e9, "unit": "GFLOP/s", "cores": 1, "kind": "port",
+           "sample": (f"lair getrf_row_major + getrs restated in C++ (-O2 -ffp-contract=off), 1 thread: "
+                      f"the first {state['next']} elimination steps of an n={n} N(0,1) matrix plus "
+                      f"{steps} single-RHS getrs at n={n}; {t_total:.1f} s of CPU work"),
+           "host": os.uname().machine, "host_cores_total": os.cpu_count()}
+    if full_n:
+        t_full = cpu_full_run(full_n, nrhs)
+        scale = (n / full_n) ** 3
+        out["full_run"] = {"n": full_n, "nrhs": nrhs, "seconds": t_full,
+                           "gflops": flops_of(full_n, nrhs) / t_full / 1e9,
+                           "what": f"complete getrf_row_major + {nrhs} single-RHS getrs at n={full_n}, 1 thread"}
+        out["extrapolated"] = {"n": n, "seconds": t_full * scale,
+                               "gflops": flops_of(n, nrhs) / (t_full * scale) / 1e9,
+                               "how": f"EXTRAPOLATED, not measured: the n={full_n} time x (n/{full_n})^3"}
+    return out
 
 
 def run_reference(args):
@@ -182,10 +213,64 @@ def run_reference(args):
 
 
 def workload_config(args):
-    return {"workload": f"plain FP64 getrf+getrs drop-in, n={args.n}, nrhs={args.nrhs}, A,B iid N(0,1) seeded",
+    return {"workload": f"plain FP64 getrf+getrs drop-in, n={args.n}, nrhs={args.nrhs}, A,B iid N(0,1) seeded "
+                        "(portable generator, lair_gb300.synthetic)",
             "n": args.n, "nrhs": args.nrhs, "mode": args.mode,
             "l2": "inputs larger than L2 (A is %.1f GiB vs 129 MB L2)" % (args.n * args.n * 8 / 2 ** 30),
             "parallelism": "replicas (one independent system per GPU)"}
+
+
+def measured_hbm_peak() -> float:
+    """HBM copy bandwidth measured on the GB300s, else the fallback."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"])
+    except (OSError, ValueError, KeyError):
+        return 6800.0
+
+
+def load_parity_fixture(n: int, nrhs: int):
+    """lair's results (the oracle's, committed under tests/golden) for the
+    seeded N(0,1) system of order n, if there is one for this size."""
+    path = os.path.join(ROOT, "tests", "golden", f"getrf_normal_n{n}.npz")
+    if not os.path.exists(path):
+        return None
+    fx = np.load(path)
+    return fx if int(fx["nrhs"]) == nrhs else None
+
+
+def parity_vs_lair(torch, n, fx, A0, LU, piv, X):
+    """Fast-mode results of the last timed step against lair's on the same
+    inputs: pivots (or the first differing step and the candidates' margin
+    there), ||PA - LU||_max / (n eps ||A||_max) on the GPU in FP64, the
+    solution's relative error against lair's for columns 0 and 1, and 2048
+    sampled entries of L\\U."""
+    p = piv.cpu().numpy().astype(np.int64)
+    ref = fx["piv"].astype(np.int64)
+    diff = np.nonzero(p != ref)[0]
+    first = int(diff[0]) if diff.size else -1
+    perm = np.arange(n)
+    for i, j in enumerate(p):
+        if j != i:
+            perm[i], perm[j] = perm[j], perm[i]
+    L = torch.tril(LU, -1)
+    L.diagonal().fill_(1.0)
+    err = (A0[torch.from_numpy(perm).cuda()] - L @ torch.triu(LU)).abs().max().item()
+    del L
+    x = X[:, :2].cpu().numpy()
+    rows = torch.from_numpy(fx["lu_rows"].astype(np.int64)).cuda()
+    cols = torch.from_numpy(fx["lu_cols"].astype(np.int64)).cuda()
+    lu_s = LU[rows, cols].cpu().numpy()
+    out = {"reference": "lair getrf_row_major + getrs (oracle, same seeded inputs; tests/golden)",
+           "pivots_identical": first < 0, "first_divergent_step": first,
+           "pa_minus_lu_over_n_eps_a": err / (n * EPS64 * A0.abs().max().item()),
+           "solution_rel_err_vs_lair": float(np.abs(x - fx["x01"]).max() / np.abs(fx["x01"]).max()),
+           "lu_sample_rel_diff": float(np.abs(lu_s - fx["lu_vals"]).max() / np.abs(fx["lu_vals"]).max()),
+           "min_relative_pivot_margin": float(np.min(fx["gap"] / fx["colmax"]))}
+    if first >= 0:
+        out["margin_at_divergence"] = float(fx["gap"][first])
+        out["allowed_margin"] = float(64 * n * EPS64 * fx["colmax"][first])
+    return out
 
 
 def read_traffic(path):
@@ -228,9 +313,23 @@ def run_ours(args):
 
     n, nrhs = args.n, args.nrhs
     lda = n
-    gen = torch.Generator(device="cuda").manual_seed(args.seed + rank)
-    A0 = torch.randn((n, n), dtype=torch.float64, device="cuda", generator=gen)
-    B0 = torch.randn((n, nrhs), dtype=torch.float64, device="cuda", generator=gen)
+    fixture = load_parity_fixture(n, nrhs)
+    if fixture is not None:
+        # the seeded inputs of lair's reference results (parity key below)
+        from lair_gb300 import synthetic
+
+        a_h = synthetic.normal_matrix(int(fixture["seed_a"]), n, n)
+        b_h = synthetic.normal_matrix(int(fixture["seed_b"]), n, nrhs)
+        A0 = torch.from_numpy(a_h).cuda()
+        B0 = torch.from_numpy(b_h).cuda()
+        inputs_match = (synthetic.digest(a_h) == str(fixture["a_digest"])
+                        and synthetic.digest(b_h) == str(fixture["b_digest"]))
+        del a_h, b_h
+    else:
+        gen = torch.Generator(device="cuda").manual_seed(args.seed + rank)
+        A0 = torch.randn((n, n), dtype=torch.float64, device="cuda", generator=gen)
+        B0 = torch.randn((n, nrhs), dtype=torch.float64, device="cuda", generator=gen)
+        inputs_match = False
     A = torch.empty_like(A0)
     X = torch.empty_like(B0)
     piv = torch.empty(n, dtype=torch.int32, device="cuda")
@@ -277,6 +376,11 @@ def run_ours(args):
     # backward error of the last solve (FP64 on the GPU)
     R = B0 - A0 @ X
     berr = (R.abs().max() / (A0.abs().sum(1).max() * X.abs().max() + B0.abs().max())).item()
+    del R
+    parity = None
+    if fixture is not None and mode == _lib.MODE_FAST:
+        parity = parity_vs_lair(torch, n, fixture, A0, A, piv, X) if inputs_match else {
+            "error": "inputs were not reproduced bit for bit; no comparison"}
 
     g = prof.get("gemm", {"ms": 0.0, "flops": 0.0, "launches": 0})
     gemm_tflops = g["flops"] / (g["ms"] * 1e-3) / 1e12 if g["ms"] else 0.0
@@ -334,6 +438,11 @@ def run_ours(args):
         torch.cuda.empty_cache()
         batched_res = run_batched(args, lib, ctx, torch)
 
+    adjoint_res = None
+    if not args.no_adjoint:
+        torch.cuda.empty_cache()
+        adjoint_res = run_adjoint(args, lib, ctx, torch)
+
     qr_res = None
     if not args.no_qr:
         torch.cuda.empty_cache()
@@ -341,17 +450,17 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_baseline(n, args.cpu_seconds)
+        cpu = cpu_baseline(n, nrhs, args.cpu_seconds, args.cpu_full_n)
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "GFLOP/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                 "config": workload_config(args), "backward_error": berr, "berr_bound": n * EPS64,
-                "berr_ok": berr <= n * EPS64, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "berr_ok": berr <= n * EPS64, "parity": parity, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                 "clocks": clocks.summary(), "gpu_launches": int(launches),
                 "kernel_profile_ms": {k: round(v["ms"], 3) for k, v in prof.items()}, "ir": ir,
-                "batched": batched_res, "qr": qr_res}
+                "batched": batched_res, "adjoint": adjoint_res, "qr": qr_res}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -430,8 +539,7 @@ def run_ir(args, lib, ctx, torch, rank):
                 "berr_ok": berr <= n * EPS64, "factor_ms": info.factor_ms, "refine_ms": info.refine_ms}
 
     results = {}
-    for prec, solver in (("fp32", "ir"), ("bf16x3", "ir"), ("bf16x3", "gmres"), ("fp32", "gmres"), ("tf32", "gmres"),
-                         ("fp16", "gmres"), ("bf16", "gmres")):
+    for prec, solver in (tuple(r.split("/")) for r in args.ir_runs.split(",")):
         headline = solver == "ir"
         results[f"{prec}/{solver}"] = measure(A, prec, solver, args.steps if headline else 1,
                                               args.warmup if headline else 1)
@@ -474,6 +582,97 @@ def run_ir(args, lib, ctx, torch, rank):
             "fp64_backward_error": fp64_berr, "best": best, "best_gflops": results[best]["gflops"],
             "speedup_vs_fp64": fp64_ms / results[best]["ms"], "berr_bound": n * EPS64,
             "kappa_sweep": sweep}
+
+
+def run_adjoint(args, lib, ctx, torch):
+    """Adjoint of the solve at n = 2048, nrhs = 8: A = N(0,1)/sqrt(n) + I,
+    B and W iid N(0,1), X = A^-1 B by getrf + getrs.  Times the FP64 backward
+    with the stored factors (lambda = A^-T W by the transposed sweeps,
+    dB = lambda, dA = -lambda X^T), the same including its factorization, and
+    the mixed-precision form (lambda by refinement on A^T, which factors A^T
+    in the low precision).  L2 (129 MB) holds the whole problem, so it is
+    flushed before every timed call (a 512 MB write); each call is timed
+    alone with CUDA events."""
+    import ctypes
+
+    from lair_gb300 import _lib
+
+    n, nrhs = args.adj_n, args.adj_nrhs
+    gen = torch.Generator(device="cuda").manual_seed(23)
+    A = torch.randn((n, n), dtype=torch.float64, device="cuda", generator=gen) / np.sqrt(n)
+    A += torch.eye(n, dtype=torch.float64, device="cuda")
+    B = torch.randn((n, nrhs), dtype=torch.float64, device="cuda", generator=gen)
+    W = torch.randn((n, nrhs), dtype=torch.float64, device="cuda", generator=gen)
+    LU = A.clone()
+    piv = torch.empty(n, dtype=torch.int32, device="cuda")
+    X = B.clone()
+    dB = torch.empty_like(B)
+    dA = torch.empty_like(A)
+    flush = torch.empty(64 << 20, dtype=torch.float64, device="cuda")
+    sing = ctypes.c_int64(0)
+    stream = torch.cuda.current_stream()
+    _lib.check(lib.luhot_dgetrf_dev(ctx, n, n, LU.data_ptr(), n, piv.data_ptr(), ctypes.byref(sing), 0), ctx)
+    _lib.check(lib.luhot_dgetrs_dev(ctx, n, nrhs, LU.data_ptr(), n, piv.data_ptr(), X.data_ptr(), nrhs, 0, 0), ctx)
+
+    def timed(fn, reps):
+        ts = []
+        for _ in range(reps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return float(np.median(ts))
+
+    def fp64_stored():
+        _lib.check(lib.luhot_dgesv_backward_dev(ctx, n, nrhs, LU.data_ptr(), n, piv.data_ptr(), X.data_ptr(), nrhs,
+                                                W.data_ptr(), nrhs, dB.data_ptr(), nrhs, dA.data_ptr(), n, 0), ctx)
+
+    LU2 = torch.empty_like(A)
+
+    def fp64_with_factor():
+        LU2.copy_(A)
+        _lib.check(lib.luhot_dgetrf_dev(ctx, n, n, LU2.data_ptr(), n, piv.data_ptr(), ctypes.byref(sing), 0), ctx)
+        fp64_stored()
+
+    info = _lib.IrInfo()
+    dB_ir, dA_ir = torch.empty_like(B), torch.empty_like(A)
+
+    def ir(prec):
+        def run():
+            rc = lib.luhot_dgesv_backward_ir_dev(ctx, n, nrhs, A.data_ptr(), n, X.data_ptr(), nrhs, W.data_ptr(), nrhs,
+                                                 dB_ir.data_ptr(), nrhs, dA_ir.data_ptr(), n,
+                                                 _lib.PRECISIONS[prec], _lib.REFINE_IR, 0.0, 50, ctypes.byref(info))
+            _lib.check(rc, ctx)
+        return run
+
+    reps = max(3, args.steps)
+    for f in (fp64_stored, fp64_with_factor):
+        f()
+    ms_stored = timed(fp64_stored, reps)
+    ms_factor = timed(fp64_with_factor, reps)
+    lam_ref = dB.clone()
+    dA_ref = dA.clone()
+    out_ir = {}
+    for prec in ("fp32", "bf16x3"):
+        ir(prec)()
+        ms = timed(ir(prec), reps)
+        out_ir[prec] = {"ms": ms, "iterations": info.iterations, "backward_error_of_lambda": info.backward_error,
+                        "dA_rel_diff_vs_fp64": float((dA_ir - dA_ref).abs().max() / dA_ref.abs().max()),
+                        "dB_rel_diff_vs_fp64": float((dB_ir - lam_ref).abs().max() / lam_ref.abs().max())}
+    # algorithmic bytes of the backward with stored factors: both triangles of
+    # the factor read once (8 n^2), dA written once (8 n^2), W, X, lambda/dB
+    # moved a few times (about 6 * 8 n nrhs)
+    byts = 16.0 * n * n + 48.0 * n * nrhs
+    del flush, LU2
+    return {"workload": f"adjoint of X = A^-1 B: n={n}, nrhs={nrhs}, A = N(0,1)/sqrt(n) + I, B, W iid N(0,1)",
+            "fp64_stored_factors_ms": ms_stored, "fp64_stored_factors_gbs": byts / (ms_stored * 1e-3) / 1e9,
+            "hbm_frac_of_measured": byts / (ms_stored * 1e-3) / 1e9 / args.hbm_peak_gbs,
+            "algorithmic_bytes": byts, "fp64_with_getrf_ms": ms_factor, "ir": out_ir,
+            "timing": "median of %d calls, L2 flushed before each" % reps}
 
 
 def run_qr(args, lib, ctx, torch):
@@ -523,9 +722,17 @@ def run_batched(args, lib, ctx, torch):
 
     from lair_gb300 import _lib, batched
 
+    world, rank, _ = dist_env()
     out = {}
     for name, dt, tdt in (("f64", np.float64, torch.float64), ("f32", np.float32, torch.float32)):
-        sizes, a0, b0 = batched.synthetic_batch(args.batch_count, seed=11, dtype=dt)
+        sizes_all, a_all, b_all = batched.synthetic_batch(args.batch_count, seed=11, dtype=dt)
+        # one contiguous slice per rank, balanced by the sum of n^3; no collective
+        s0, s1 = batched.shard_by_work(sizes_all, world)[rank]
+        aoff_all = np.concatenate([[0], np.cumsum(sizes_all.astype(np.int64) ** 2)])
+        boff_all = np.concatenate([[0], np.cumsum(sizes_all.astype(np.int64))])
+        sizes = sizes_all[s0:s1]
+        a0 = a_all[aoff_all[s0]:aoff_all[s1]]
+        b0 = b_all[boff_all[s0]:boff_all[s1]]
         solver = batched.BatchSolver(sizes, dtype=dt, mode="fast")
         A0 = torch.from_numpy(a0).cuda()
         B0 = torch.from_numpy(b0).cuda()
@@ -552,6 +759,11 @@ def run_batched(args, lib, ctx, torch):
         e1.record(stream)
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / args.steps
+        ms_all = ms
+        if world > 1:
+            tt = torch.tensor([ms], dtype=torch.float64, device="cuda")
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            ms_all = float(tt.item())
         # worst backward error over the batch (FP64 check on the host)
         x = B.cpu().numpy()
         worst, ao, bo = 0.0, 0, 0
@@ -585,11 +797,15 @@ def run_batched(args, lib, ctx, torch):
         loop_s = time.perf_counter() - t0
         loop_rate = len(sample) / loop_s
         fl = float(np.sum(2.0 / 3.0 * sizes.astype(np.float64) ** 3 + 2.0 * sizes.astype(np.float64) ** 2))
-        out[name] = {"systems": len(sizes), "ms_per_batch": ms, "systems_per_s": len(sizes) / (ms * 1e-3),
-                     "gflops": fl / (ms * 1e-3) / 1e9, "worst_backward_error": worst,
+        fl_all = float(np.sum(2.0 / 3.0 * sizes_all.astype(np.float64) ** 3 + 2.0 * sizes_all.astype(np.float64) ** 2))
+        out[name] = {"systems": len(sizes_all), "systems_this_rank": len(sizes), "ranks": world,
+                     "ms_per_batch": ms_all, "systems_per_s": len(sizes_all) / (ms_all * 1e-3),
+                     "gflops": fl_all / (ms_all * 1e-3) / 1e9, "worst_backward_error_this_rank": worst,
                      "loop_single_system_systems_per_s": loop_rate,
                      "loop_sample": f"{len(sample)} systems drawn from the batch, getrf_dev + getrs_dev each",
                      "speedup_vs_loop": (len(sizes) / (ms * 1e-3)) / loop_rate, "autotune_s": tune_s,
+                     "sharding": "contiguous slices balanced by sum n^3, one per rank, no collective; "
+                                 "aggregate rate = all systems / slowest rank's time",
                      "tuning": solver.tuning()}
         del A0, B0, A, B
     return out
@@ -608,18 +824,32 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--cpu-full-n", type=int, default=4096,
+                    help="order of the complete CPU run beside the sample (0: skip)")
     ap.add_argument("--ref-elim-steps", type=int, default=4)
     ap.add_argument("--no-ir", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-qr", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--adj-n", type=int, default=2048)
+    ap.add_argument("--adj-nrhs", type=int, default=8)
+    ap.add_argument("--hbm-peak-gbs", type=float, default=None,
+                    help="HBM roofline (default: MEASURED_PEAKS.json, else 6800)")
     ap.add_argument("--qr-n", type=int, default=4096)
     ap.add_argument("--batch-count", type=int, default=10000)
     ap.add_argument("--batch-loop-sample", type=int, default=300)
     ap.add_argument("--ir-n", type=int, default=16384)
     ap.add_argument("--ir-kappa", type=float, default=1e6)
+    ap.add_argument("--ir-runs", default="fp32/ir,bf16x3/ir,bf16x3/gmres,fp32/gmres,tf32/gmres,fp16/gmres,bf16/gmres",
+                    help="precision/solver pairs of the refinement leg, comma separated")
     ap.add_argument("--no-ir-sweep", action="store_true",
                     help="skip the kappa = 1e2 and 1e4 runs of the refinement leg")
     args = ap.parse_args()
+    world, rank, _ = dist_env()
+    if args.gpus != world and rank == 0:
+        print(f"bench: --gpus {args.gpus} but WORLD_SIZE={world}; measuring {world} rank(s)", file=sys.stderr)
+    if args.hbm_peak_gbs is None:
+        args.hbm_peak_gbs = measured_hbm_peak()
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -50,6 +50,8 @@ def lib():
             getattr(L, name).restype = _i64
         L.oracle_dgetrf_row_major_range.argtypes = [_i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64]
         L.oracle_dgetrf_row_major_range.restype = _i64
+        L.oracle_dgetrf_row_major_blocked.argtypes = [_i64, _i64, _vp, _i64, _vp, _i64, ctypes.c_int, _vp, _vp]
+        L.oracle_dgetrf_row_major_blocked.restype = _i64
         L.oracle_dgetrf_recursive.argtypes = [_i64, _i64, _vp, _i64, _i64, _vp, _vp]
         L.oracle_dgetrf_recursive.restype = ctypes.c_int
         for name in ("oracle_dgetrs", "oracle_sgetrs"):
@@ -155,6 +157,28 @@ def getrf_row_major_range(a: np.ndarray, piv: np.ndarray, step_begin: int, step_
     rs, cs = _estrides(a)
     s = lib().oracle_dgetrf_row_major_range(m, n, _ptr(a), rs, cs, _ptr(piv), step_begin, step_end)
     return _singular(s)
+
+
+def getrf_row_major_blocked(a: np.ndarray, block: int = 64, threads: int = 0, margins: bool = False):
+    """getrf_row_major (src/lapack/getrf.rs:46-120) on a C-order float64 array,
+    bit-identical, in blocks of ``block`` steps on ``threads`` threads (0: all
+    cores), for large fixtures.  Returns (pivots, singular) or, with
+    ``margins``, (pivots, singular, colmax, gap): per step the largest pivot
+    candidate |a| and its margin over the second largest."""
+    if a.dtype != np.float64 or not a.flags.c_contiguous and a.strides[1] != a.itemsize:
+        raise TypeError("blocked oracle: float64 with unit column stride")
+    m, n = a.shape
+    lda = a.strides[0] // a.itemsize if m > 1 else n
+    k = min(m, n)
+    piv = np.arange(k, dtype=np.uint64)
+    colmax = np.zeros(max(k, 1)) if margins else None
+    gap = np.zeros(max(k, 1)) if margins else None
+    threads = threads or (os.cpu_count() or 1)
+    s = lib().oracle_dgetrf_row_major_blocked(m, n, _ptr(a), lda, _ptr(piv), block, threads,
+                                              _ptr(colmax) if margins else None, _ptr(gap) if margins else None)
+    if margins:
+        return piv, _singular(s), colmax[:k], gap[:k]
+    return piv, _singular(s)
 
 
 def getrf_col_major(a: np.ndarray):

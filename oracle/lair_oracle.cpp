@@ -10,6 +10,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <functional>
+#include <thread>
 #include <limits>
 #include <vector>
 
@@ -98,6 +100,136 @@ int64_t getrf_row_major(int64_t m, int64_t n, T* a, int64_t rs, int64_t cs, uint
   const int64_t dim_min = std::min(m, n);
   const int64_t steps = (max_steps < 0) ? dim_min : std::min(dim_min, max_steps);
   return getrf_row_major_range<T>(m, n, a, rs, cs, piv, 0, steps);
+}
+
+// The same elimination as getrf_row_major_range for a C-order array (row
+// stride lda, column stride 1), reordered across elements but never within
+// one, so that large fixtures can be made in minutes: every element receives
+// lair's updates a[i][c] -= l[i][t] * u[t][c] in increasing t, each product
+// and difference rounded apart, with the same multipliers (scaled by the
+// same reciprocal) and the same pivot searches, interchanges and singular
+// steps, so the result is bit-identical to the unblocked order.  Steps run
+// in blocks of w: the block's columns are eliminated step by step (with the
+// full-row interchanges lair makes, applied to the other columns once the
+// block's steps are known, since nothing reads those columns meanwhile);
+// then the block's rows of the columns to the right receive their updates in
+// step order (each row t is final before rows below use it), and the rows
+// below receive the block's w updates per element, split over threads.
+// Optionally records, per step, the largest candidate |a| and the gap to the
+// second largest (the margin by which the pivot won).
+template <typename T>
+int64_t getrf_row_major_blocked(int64_t m, int64_t n, T* a, int64_t lda, uint64_t* piv, int64_t w,
+                                int nthreads, double* colmax, double* gap) {
+  const int64_t dim_min = std::min(m, n);
+  if (w < 1) w = 64;
+  if (nthreads < 1) nthreads = 1;
+  int64_t singular = -1;
+  std::vector<char> skip((size_t)std::max<int64_t>(dim_min, 1), 0);
+  auto run_threads = [&](int64_t count, const std::function<void(int64_t, int64_t)>& fn) {
+    const int64_t nt = std::min<int64_t>(nthreads, std::max<int64_t>(count, 1));
+    if (nt <= 1) {
+      fn(0, count);
+      return;
+    }
+    std::vector<std::thread> th;
+    for (int64_t t = 0; t < nt; ++t) {
+      const int64_t lo = count * t / nt, hi = count * (t + 1) / nt;
+      th.emplace_back([&fn, lo, hi] { fn(lo, hi); });
+    }
+    for (auto& x : th) x.join();
+  };
+  for (int64_t k0 = 0; k0 < dim_min; k0 += w) {
+    const int64_t kend = std::min(k0 + w, dim_min);
+    const int64_t pend = std::min(k0 + w, n);
+    // Block columns [k0, pend), every row, step by step.
+    for (int64_t ul = k0; ul < kend; ++ul) {
+      T max_val = T(0), second = T(0);
+      int64_t max_idx = 0;
+      for (int64_t i = 0; i < m - ul; ++i) {  // iamax, strict `>`; NaN never wins
+        const T val = std::fabs(a[(ul + i) * lda + ul]) + T(0);
+        if (val > max_val) {
+          second = max_val;
+          max_val = val;
+          max_idx = i;
+        } else if (val > second) {
+          second = val;
+        }
+      }
+      if (colmax) colmax[ul] = (double)max_val;
+      if (gap) gap[ul] = (double)(max_val - second);
+      piv[ul] = (uint64_t)ul;
+      if (max_idx != 0) {
+        const int64_t r = max_idx + ul;
+        piv[ul] = (uint64_t)r;
+        for (int64_t c = k0; c < pend; ++c) std::swap(a[ul * lda + c], a[r * lda + c]);
+      }
+      if (max_val == T(0)) {
+        singular = max_idx + ul;
+        skip[(size_t)ul] = 1;
+        continue;
+      }
+      const T pivot_recip = T(1) / a[ul * lda + ul];
+      const T* urow = a + ul * lda;
+      for (int64_t j = ul + 1; j < m; ++j) {
+        T* row = a + j * lda;
+        row[ul] *= pivot_recip;
+        const T ratio = row[ul];
+        for (int64_t c = ul + 1; c < pend; ++c) {
+          const T elem = ratio * urow[c];
+          row[c] -= elem;
+        }
+      }
+    }
+    // The block's interchanges, on the columns outside the block, in order.
+    for (int64_t ul = k0; ul < kend; ++ul) {
+      const int64_t r = (int64_t)piv[ul];
+      if (r == ul) continue;
+      for (int64_t c = 0; c < k0; ++c) std::swap(a[ul * lda + c], a[r * lda + c]);
+      for (int64_t c = pend; c < n; ++c) std::swap(a[ul * lda + c], a[r * lda + c]);
+    }
+    if (pend >= n) continue;
+    constexpr int64_t kTile = 256;
+    const int64_t ncols = n - pend, ntiles = (ncols + kTile - 1) / kTile;
+    // The block's own rows, columns to the right: row t is final before the
+    // rows below it use it.
+    run_threads(ntiles, [&](int64_t lo, int64_t hi) {
+      for (int64_t tile = lo; tile < hi; ++tile) {
+        const int64_t c0 = pend + tile * kTile, c1 = std::min(n, c0 + kTile);
+        for (int64_t t = k0; t < kend; ++t) {
+          if (skip[(size_t)t]) continue;
+          const T* urow = a + t * lda;
+          for (int64_t i = t + 1; i < kend; ++i) {
+            T* row = a + i * lda;
+            const T ratio = row[t];
+            for (int64_t c = c0; c < c1; ++c) {
+              const T elem = ratio * urow[c];
+              row[c] -= elem;
+            }
+          }
+        }
+      }
+    });
+    // The rows below the block: the block's updates in step order.
+    const int64_t rows = m - kend;
+    run_threads(rows, [&](int64_t lo, int64_t hi) {
+      for (int64_t c0 = pend; c0 < n; c0 += kTile) {
+        const int64_t c1 = std::min(n, c0 + kTile);
+        for (int64_t i = kend + lo; i < kend + hi; ++i) {
+          T* row = a + i * lda;
+          for (int64_t t = k0; t < kend; ++t) {
+            if (skip[(size_t)t]) continue;
+            const T ratio = row[t];
+            const T* urow = a + t * lda;
+            for (int64_t c = c0; c < c1; ++c) {
+              const T elem = ratio * urow[c];
+              row[c] -= elem;
+            }
+          }
+        }
+      }
+    });
+  }
+  return singular;
 }
 
 // src/blas/dot.rs:39-133: four partial sums over blocks of four, combined as
@@ -512,6 +644,11 @@ int64_t oracle_dgetrf_row_major_range(int64_t m, int64_t n, double* a, int64_t r
   const int64_t dim_min = std::min(m, n);
   return getrf_row_major_range<double>(m, n, a, rs, cs, piv, std::max<int64_t>(0, step_begin),
                                        std::min(dim_min, step_end));
+}
+
+int64_t oracle_dgetrf_row_major_blocked(int64_t m, int64_t n, double* a, int64_t lda, uint64_t* piv,
+                                        int64_t w, int nthreads, double* colmax, double* gap) {
+  return getrf_row_major_blocked<double>(m, n, a, lda, piv, w, nthreads, colmax, gap);
 }
 
 int64_t oracle_dgetrf_col_major(int64_t m, int64_t n, double* a, int64_t rs, int64_t cs,

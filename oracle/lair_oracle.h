@@ -49,6 +49,14 @@ int64_t oracle_sgetrf_row_major(int64_t m, int64_t n, float* a, int64_t rs, int6
 int64_t oracle_dgetrf_row_major_range(int64_t m, int64_t n, double* a, int64_t rs, int64_t cs,
                                       uint64_t* piv, int64_t step_begin, int64_t step_end);
 
+/* getrf_row_major's arithmetic, bit for bit, for a C-order array with row
+ * stride lda, in blocks of w steps with the updates of the rows below a
+ * block split over nthreads threads (for fixtures at large n).  piv is
+ * written in full.  colmax / gap (may be NULL) receive, per step, the largest
+ * candidate |a| and its margin over the second largest. */
+int64_t oracle_dgetrf_row_major_blocked(int64_t m, int64_t n, double* a, int64_t lda, uint64_t* piv,
+                                        int64_t w, int nthreads, double* colmax, double* gap);
+
 /* src/lapack/getrf.rs:128-213 (getrf_col_major, left-looking Crout). */
 int64_t oracle_dgetrf_col_major(int64_t m, int64_t n, double* a, int64_t rs, int64_t cs,
                                 uint64_t* piv);
