@@ -22,7 +22,12 @@
  *    (row-major getrf order, src/lapack/getrf.rs:46-120, and getrs order,
  *    src/lapack/getrs.rs:12-38); LUHOT_MODE_FAST uses the FP64 tensor cores
  *    and FMA, with identical pivots wherever the pivot candidates are
- *    distinct and a backward error of the same order.
+ *    distinct and a backward error of the same order.  For a host array
+ *    that is not in ndarray's standard layout (F order, negative strides,
+ *    padded row views) lair uses its column-major order
+ *    (src/lapack/getrf.rs:20-26, 128-213); exact mode follows that order for
+ *    at most 4096 rows and returns LUHOT_ERR_UNSUPPORTED beyond, never a
+ *    different order.
  *  - A context is safe to share between threads: calls on one context are
  *    serialised by a mutex.  Use one context per thread for concurrency.
  */
@@ -167,6 +172,15 @@ typedef struct luhot_ir_info {
 int luhot_dgesv_ir_dev(luhot_ctx* ctx, int64_t n, int64_t nrhs, const double* d_a, int64_t lda,
                        const double* d_b, int64_t ldb, double* d_x, int64_t ldx, int precision,
                        int solver, double tol, int max_iter, luhot_ir_info* info);
+/* The low-precision factorization of the solves above, on its own: LU with
+ * partial pivoting of an m x n row-major FP32 device matrix (lda, in place;
+ * int32 pivots), FP32 panels and triangular solves, Schur updates in the
+ * given LUHOT_PREC_* (BF16 / FP16 operands scaled per panel by powers of two,
+ * TF32 operands rounded to nearest, FP32 accumulation).  For callers that
+ * keep the preconditioner themselves, and for measuring its quality.  No
+ * lair counterpart. */
+int luhot_sgetrf_mixed_dev(luhot_ctx* ctx, int64_t m, int64_t n, float* d_a, int64_t lda, int32_t* d_piv,
+                           int precision, int64_t* singular);
 /* Host-buffer form of luhot_dgesv_ir_dev (any strides). */
 int luhot_dgesv_ir(luhot_ctx* ctx, int64_t n, int64_t nrhs, const double* a, int64_t rs, int64_t cs,
                    const double* b, int64_t b_rs, int64_t b_cs, double* x, int64_t x_rs, int64_t x_cs,

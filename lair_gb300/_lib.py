@@ -56,6 +56,7 @@ SIGNATURES = {
     "luhot_dgetrs_dev": (_i32, [_vp, _i64, _i64, _vp, _i64, _vp, _vp, _i64, _i32, _i32]),
     "luhot_sgetrs_dev": (_i32, [_vp, _i64, _i64, _vp, _i64, _vp, _vp, _i64, _i32, _i32]),
     "luhot_dgesv_ir_dev": (_i32, [_vp, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _i32, _i32, _dbl, _i32, _vp]),
+    "luhot_sgetrf_mixed_dev": (_i32, [_vp, _i64, _i64, _vp, _i64, _vp, _i32, _vp]),
     "luhot_dgesv_ir": (_i32, [_vp, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _i64, _i32, _i32, _dbl,
                               _i32, _vp]),
     "luhot_dgesv_backward": (_i32, [_vp, _i64, _i64, _vp, _i64, _i64, _vp, _vp, _i64, _i64, _vp, _i64, _i64, _vp,

@@ -327,6 +327,19 @@ HostPin::~HostPin() {
   }
 }
 
+// ndarray 0.17's ArrayBase::is_contiguous for two axes: the elements fill
+// one block of memory in C or F order, strides of either sign (axes of
+// length 1 take any stride).  lair's equation::solve copies A with to_owned
+// (src/equation.rs:54), which keeps the strides of such an array and makes
+// any other array standard.
+static bool ndarray_contiguous(int64_t m, int64_t n, int64_t rs, int64_t cs) {
+  if (m == 0 || n == 0) return true;
+  const int64_t ars = rs < 0 ? -rs : rs, acs = cs < 0 ? -cs : cs;
+  if (m == 1) return n == 1 || acs == 1;
+  if (n == 1) return ars == 1;
+  return (acs == 1 && ars == n) || (ars == 1 && acs == m);
+}
+
 static bool dims_ok(int64_t m, int64_t n) {
   return m >= 0 && n >= 0 && m < (int64_t)INT32_MAX && n < (int64_t)INT32_MAX &&
          (m == 0 || n == 0 || m * n / n == m);
@@ -463,7 +476,7 @@ int luhot_create(luhot_ctx** out, int device) {
   ctx->stream = ctx->own_stream;
   ok = ok && cudaMalloc(&ctx->d_status, sizeof(DeviceStatus)) == cudaSuccess;
   ok = ok && cudaMallocHost(&ctx->h_status, sizeof(DeviceStatus)) == cudaSuccess;
-  ok = ok && cudaMallocHost(&ctx->h_scalars, 256 * sizeof(double)) == cudaSuccess;
+  ok = ok && cudaMallocHost(&ctx->h_scalars, kIrScalarSlots * sizeof(double)) == cudaSuccess;
   ok = ok && cudaMalloc(&ctx->panel_scratch, kPanelScratchBytes) == cudaSuccess;
   if (!ok || ctx->num_sms > kMaxPanelCtas) {
     cudaGetLastError();
@@ -585,11 +598,34 @@ int luhot_dgesv(luhot_ctx* ctx, int64_t n, int64_t nrhs, const double* a, int64_
   double* d_a = static_cast<double*>(ctx->work[0].ptr);
   double* d_b = static_cast<double*>(ctx->work[2].ptr);
   int* d_piv = static_cast<int*>(ctx->piv_buf.ptr);
+  int64_t sing = -1;
+  if (mode == LUHOT_MODE_EXACT && getrf_uses_colmajor(n, n, rs, cs) && ndarray_contiguous(n, n, rs, cs)) {
+    // lair's copy of a contiguous non-standard array keeps its layout, so
+    // getrf factors it in the column-major order (src/lapack/getrf.rs:20-26).
+    std::vector<double> colmajor((size_t)n * n);
+    for (int64_t j = 0; j < n; ++j)
+      for (int64_t i = 0; i < n; ++i) colmajor[(size_t)j * n + i] = a[i * rs + j * cs];
+    std::vector<uint64_t> hpiv((size_t)n);
+    rc = getrf_colmajor_host<double>(ctx, n, n, colmajor.data(), 1, n, hpiv.data(), &sing);
+    if (rc) return rc;
+    if (sing >= 0) return set_error(ctx, LUHOT_ERR_SINGULAR, "`a` is a singular matrix");
+    rc = stage_in<double>(ctx, colmajor.data(), n, n, 1, n, d_a, lda, ctx->work[1]);
+    if (rc) return rc;
+    std::vector<int> hp((size_t)n);
+    for (int64_t i = 0; i < n; ++i) hp[(size_t)i] = (int)hpiv[(size_t)i];
+    LUHOT_CUDA_TRY(ctx, cudaMemcpyAsync(d_piv, hp.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice,
+                                        ctx->stream));
+    LUHOT_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));  // colmajor and hp go out of scope
+    rc = stage_in<double>(ctx, b, n, nrhs, b_rs, b_cs, d_b, nrhs, ctx->work[1]);
+    if (rc) return rc;
+    rc = getrs_device<double>(ctx, (int)n, (int)nrhs, d_a, lda, d_piv, d_b, nrhs, d_b, nrhs, 0, mode);
+    if (rc) return rc;
+    return stage_out<double>(ctx, d_b, nrhs, x, n, nrhs, x_rs, x_cs, ctx->work[1]);
+  }
   rc = stage_in<double>(ctx, a, n, n, rs, cs, d_a, lda, ctx->work[1]);
   if (rc) return rc;
   rc = stage_in<double>(ctx, b, n, nrhs, b_rs, b_cs, d_b, nrhs, ctx->work[1]);
   if (rc) return rc;
-  int64_t sing = -1;
   rc = getrf_device<double>(ctx, (int)n, (int)n, d_a, lda, d_piv, mode, &sing);
   if (rc) return rc;
   if (sing >= 0) return set_error(ctx, LUHOT_ERR_SINGULAR, "`a` is a singular matrix");
@@ -616,6 +652,16 @@ int luhot_sgetrf_dev(luhot_ctx* ctx, int64_t m, int64_t n, float* d_a, int64_t l
   if (!dims_ok(m, n)) return set_error(ctx, LUHOT_ERR_INVALID_ARG, "getrf: invalid dimensions");
   if (std::min(m, n) > 0 && (!d_a || !d_piv)) return set_error(ctx, LUHOT_ERR_INVALID_ARG, "getrf: null pointer");
   return getrf_device<float>(ctx, (int)m, (int)n, d_a, lda, d_piv, mode, singular);
+}
+
+int luhot_sgetrf_mixed_dev(luhot_ctx* ctx, int64_t m, int64_t n, float* d_a, int64_t lda, int32_t* d_piv,
+                           int precision, int64_t* singular) {
+  LUHOT_NVTX_FN();
+  if (!ctx) return LUHOT_ERR_INVALID_ARG;
+  Guard g(ctx);
+  if (!dims_ok(m, n)) return set_error(ctx, LUHOT_ERR_INVALID_ARG, "getrf: invalid dimensions");
+  if (std::min(m, n) > 0 && (!d_a || !d_piv)) return set_error(ctx, LUHOT_ERR_INVALID_ARG, "getrf: null pointer");
+  return getrf_mixed_device(ctx, (int)m, (int)n, d_a, lda, d_piv, precision, singular);
 }
 
 int luhot_dgetrs_dev(luhot_ctx* ctx, int64_t n, int64_t nrhs, const double* d_lu, int64_t lda,

@@ -91,13 +91,33 @@ int factor_create(luhot_ctx* ctx, int64_t m, int64_t n, const T* a, int64_t rs, 
   T* lu = static_cast<T*>(f->d_lu);
   if (k > 0) {
     HostPin pin_a(ctx, d_a ? nullptr : a, m, n, rs, cs, sizeof(T));
-    if (d_a) {
-      rc = copy_2d(ctx, lu, f->lda * sizeof(T), d_a, ld_in * sizeof(T), n * sizeof(T), m, cudaMemcpyDeviceToDevice);
-    } else {
-      rc = stage_in<T>(ctx, a, m, n, rs, cs, lu, f->lda, ctx->work[1]);
-    }
     int64_t sing = -1;
-    if (!rc) rc = getrf_device<T>(ctx, (int)m, (int)n, lu, f->lda, f->d_piv, mode, &sing);
+    if (!d_a && mode == LUHOT_MODE_EXACT && getrf_uses_colmajor(m, n, rs, cs)) {
+      // lair factors a non-standard layout in its column-major order
+      // (src/lapack/getrf.rs:20-26, 128-213): run that order on an F-order
+      // copy, then keep the factored copy on the device.
+      std::vector<T> colmajor((size_t)m * n);
+      for (int64_t j = 0; j < n; ++j)
+        for (int64_t i = 0; i < m; ++i) colmajor[(size_t)j * m + i] = a[i * rs + j * cs];
+      rc = getrf_colmajor_host<T>(ctx, m, n, colmajor.data(), 1, m, piv, &sing);
+      if (!rc) rc = stage_in<T>(ctx, colmajor.data(), m, n, 1, m, lu, f->lda, ctx->work[1]);
+      if (!rc) {
+        std::vector<int> hp((size_t)k);
+        for (int64_t i = 0; i < k; ++i) hp[(size_t)i] = (int)piv[i];
+        if (cudaMemcpyAsync(f->d_piv, hp.data(), (size_t)k * sizeof(int), cudaMemcpyHostToDevice, ctx->stream) !=
+                cudaSuccess ||
+            cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+          rc = set_error(ctx, LUHOT_ERR_CUDA, std::string("factor: ") + cudaGetErrorString(cudaGetLastError()));
+      }
+    } else {
+      if (d_a) {
+        rc = copy_2d(ctx, lu, f->lda * sizeof(T), d_a, ld_in * sizeof(T), n * sizeof(T), m,
+                     cudaMemcpyDeviceToDevice);
+      } else {
+        rc = stage_in<T>(ctx, a, m, n, rs, cs, lu, f->lda, ctx->work[1]);
+      }
+      if (!rc) rc = getrf_device<T>(ctx, (int)m, (int)n, lu, f->lda, f->d_piv, mode, &sing);
+    }
     if (!rc && solvable) rc = getrs_perm(ctx, f->d_piv, (int)m, f->d_perm);
     if (!rc && f->d_dinv) {
       T* dl = static_cast<T*>(f->d_dinv);

@@ -246,9 +246,7 @@ bool standard_layout(int64_t m, int64_t n, int64_t rs, int64_t cs) {
 
 }  // namespace
 
-bool getrf_uses_colmajor(int64_t m, int64_t n, int64_t rs, int64_t cs) {
-  return !standard_layout(m, n, rs, cs) && m <= kCmMaxRows;
-}
+bool getrf_uses_colmajor(int64_t m, int64_t n, int64_t rs, int64_t cs) { return !standard_layout(m, n, rs, cs); }
 
 template <typename T>
 int getrf_colmajor_host(luhot_ctx* ctx, int64_t m, int64_t n, T* a, int64_t rs, int64_t cs, uint64_t* piv,
@@ -256,7 +254,10 @@ int getrf_colmajor_host(luhot_ctx* ctx, int64_t m, int64_t n, T* a, int64_t rs, 
   const int64_t k = std::min(m, n);
   if (singular) *singular = -1;
   if (k == 0) return LUHOT_OK;
-  if (m > kCmMaxRows) return set_error(ctx, LUHOT_ERR_UNSUPPORTED, "column-major exact path: too many rows");
+  if (m > kCmMaxRows)
+    return set_error(ctx, LUHOT_ERR_UNSUPPORTED,
+                     "exact mode on a non-standard layout (lair's column-major order) takes at most " +
+                         std::to_string(kCmMaxRows) + " rows; use fast mode or a C-order array");
   const int64_t ld = (m + 31) / 32 * 32;
   int rc = ensure_buf(ctx, ctx->work[0], (size_t)ld * n * sizeof(T));
   if (rc) return rc;

@@ -287,7 +287,9 @@ int getrs_apply(luhot_ctx* ctx, int n, int nrhs, const T* lu, int64_t lda, const
   // 16 right-hand sides).
   auto sweep = [&](bool lower, bool unit, bool tr, bool ex) -> int {
     prof_begin(ctx, kProfTrsv);
-    const T* dinv = (ex || tr) ? nullptr : (lower ? dinv_l : dinv_u);
+    // op(A) lower: L, or U^T whose diagonal blocks invert to (D_U^-1)^T;
+    // op(A) upper: U, or L^T (the kernel reads a given inverse transposed).
+    const T* dinv = ex ? nullptr : ((lower != tr) ? dinv_l : dinv_u);
     cudaError_t e = launch_trsv_syncfree<T>(stream, lu, lda, w, ldw, n, nrhs, lower, unit, tr, ex, flags, ticket,
                                             ctx->d_status, dinv);
     prof_end(ctx, kProfTrsv, (double)n * n * nrhs, ((double)n * n / 2 + 2.0 * total) * sizeof(T));
@@ -351,11 +353,12 @@ int getrs_device(luhot_ctx* ctx, int n, int nrhs, const T* lu, int64_t lda, cons
   // Work in a private buffer so that x may alias b.
   rc = ensure_buf(ctx, ctx->work[3], (size_t)n * nrhs * sizeof(T));
   if (rc) return rc;
-  // Fast untransposed solves use the inverses of the diagonal blocks; one
-  // small launch (64 threads per block) against two n^2 sweeps.
+  // Fast solves use the inverses of the diagonal blocks (read transposed by
+  // the transposed sweeps); one small launch (64 threads per block) against
+  // two n^2 sweeps.
   T* dinv_l = nullptr;
   T* dinv_u = nullptr;
-  if (!trans && mode == LUHOT_MODE_FAST) {
+  if (mode == LUHOT_MODE_FAST) {
     const size_t ne = trsv_inverse_elems(n);
     rc = ensure_buf(ctx, ctx->dinv_buf, 2 * ne * sizeof(T));
     if (rc) return rc;

@@ -215,11 +215,16 @@ __global__ void ir_combine_kernel(const double* __restrict__ V, int k, const dou
 // ---------------------------------------------------------------------------
 namespace {
 
-constexpr int kGmresRestart = 120;
+// Krylov dimension before a restart.  For the kappa = 1e4 systems of the
+// benchmark with 11-bit (TF32 / FP16) factors, unrestarted GMRES needs about
+// 25, 35, 51 and 88 iterations at n = 512 ... 4096 (it grows like n^0.7), so
+// about 250 at n = 16384; restarting every 120 iterations stalled there.
+constexpr int kGmresRestart = 400;
 constexpr double kGmresTol = 1e-6;  // relative reduction of the preconditioned residual per solve
 
 // Device scalars.
 enum Sc : int { kAnorm = 0, kBnorm, kRnorm, kXnorm, kVscale, kNrm2, kH = 8 };
+static_assert(kH + kGmresRestart + 1 <= kIrScalarSlots, "scalar slots hold one Hessenberg column");
 
 template <typename Tlo>
 struct IrRun {
@@ -434,7 +439,7 @@ static int ir_setup(luhot_ctx* ctx, int n, const double* a, int64_t lda, IrRun<f
   rc = ensure_buf(ctx, ctx->ir_buf[1], vecs * (2 + kGmresRestart + 1) + 3 * (size_t)n * sizeof(float) + 4096);
   if (rc) return rc;
   const size_t idx_ints = (2 * (size_t)n + 63) / 64 * 64;  // pivots + permutation, 256-byte aligned end
-  rc = ensure_buf(ctx, ctx->ir_buf[2], idx_ints * sizeof(int) + 256 * sizeof(double));
+  rc = ensure_buf(ctx, ctx->ir_buf[2], idx_ints * sizeof(int) + kIrScalarSlots * sizeof(double));
   if (rc) return rc;
   s.ctx = ctx;
   s.n = n;
@@ -469,15 +474,7 @@ static int ir_factor(IrRun<float>& s, int precision, luhot_ir_info* info) {
   int rc = s.launch_check("ir convert");
   if (rc) return rc;
   int64_t sing = -1;
-  if (precision == LUHOT_PREC_FP32) {
-    rc = getrf_device<float>(ctx, n, n, s.lu, s.ldlo, s.piv, LUHOT_MODE_FAST, &sing);
-  } else {
-    const int kind = precision == LUHOT_PREC_BF16     ? kTcBF16
-                     : precision == LUHOT_PREC_FP16   ? kTcFP16
-                     : precision == LUHOT_PREC_BF16X3 ? kTcBF16x3
-                                                      : kTcTF32;
-    rc = getrf_device_tc(ctx, n, n, s.lu, s.ldlo, s.piv, kind, &sing);
-  }
+  rc = getrf_mixed_device(ctx, n, n, s.lu, s.ldlo, s.piv, precision, &sing);
   if (rc) return rc;
   info->singular = sing;
   if (sing >= 0) return set_error(ctx, LUHOT_ERR_SINGULAR, "the low-precision factor is singular");
@@ -558,6 +555,20 @@ static int ir_refine(IrRun<float>& s, const double* b, double* x, int solver, do
   info->backward_error = std::max(info->backward_error, berr);
   info->converged = info->converged && converged;
   return LUHOT_OK;
+}
+
+int getrf_mixed_device(luhot_ctx* ctx, int m, int n, float* a, int64_t lda, int* piv, int precision,
+                       int64_t* singular) {
+  if (m < 0 || n < 0 || lda < std::max(1, n)) return set_error(ctx, LUHOT_ERR_INVALID_ARG, "getrf: bad shape or lda");
+  if (precision == LUHOT_PREC_FP32) return getrf_device<float>(ctx, m, n, a, lda, piv, LUHOT_MODE_FAST, singular);
+  if (precision != LUHOT_PREC_BF16 && precision != LUHOT_PREC_FP16 && precision != LUHOT_PREC_TF32 &&
+      precision != LUHOT_PREC_BF16X3)
+    return set_error(ctx, LUHOT_ERR_INVALID_ARG, "getrf: unknown precision");
+  const int kind = precision == LUHOT_PREC_BF16     ? kTcBF16
+                   : precision == LUHOT_PREC_FP16   ? kTcFP16
+                   : precision == LUHOT_PREC_BF16X3 ? kTcBF16x3
+                                                    : kTcTF32;
+  return getrf_device_tc(ctx, m, n, a, lda, piv, kind, singular);
 }
 
 int gesv_ir_device(luhot_ctx* ctx, int n, int nrhs, const double* a, int64_t lda, const double* b, int64_t ldb,

@@ -33,6 +33,9 @@ constexpr size_t kPanelSlotBytes = 2 * (size_t)kMaxPanelCtas * kPanelSlotWords *
 // source) pairs and their count.
 constexpr size_t kPanelMovesBytes = (4 * (size_t)kMaxPanelWidth + 64) * sizeof(int);
 constexpr size_t kPanelScratchBytes = kPanelSlotBytes + kPanelMovesBytes;
+// Scalars the refinement keeps on the device and reads back (norms and one
+// column of the GMRES Hessenberg matrix): this many doubles on each side.
+constexpr int kIrScalarSlots = 512;
 
 // Grow-only device buffer.
 struct DevBuf {
@@ -118,12 +121,19 @@ int getrf_device(luhot_ctx* ctx, int m, int n, T* a, int64_t lda, int* piv, int 
 // BF16 / FP16 / TF32 operands (TcKind) and FP32 accumulation; panel width 128.
 int getrf_device_tc(luhot_ctx* ctx, int m, int n, float* a, int64_t lda, int* piv, int tc_kind, int64_t* singular);
 
+// The low-precision LU of the mixed-precision solves: FP32 storage and
+// panels, Schur updates per LUHOT_PREC_* (FP32 CUDA cores or tcgen05).
+int getrf_mixed_device(luhot_ctx* ctx, int m, int n, float* a, int64_t lda, int* piv, int precision,
+                       int64_t* singular);
+
 int gesv_ir_device(luhot_ctx* ctx, int n, int nrhs, const double* a, int64_t lda, const double* b, int64_t ldb,
                    double* x, int64_t ldx, int precision, int solver, double tol, int max_iter,
                    luhot_ir_info* info);
 
 // lair's getrf_col_major order (non-standard layouts, exact mode): true when
-// the array is not in ndarray's standard layout and has at most 4096 rows.
+// the array is not in ndarray's standard layout (lair's dispatch predicate,
+// src/lapack/getrf.rs:20-26).  getrf_colmajor_host takes at most 4096 rows
+// and returns LUHOT_ERR_UNSUPPORTED beyond.
 bool getrf_uses_colmajor(int64_t m, int64_t n, int64_t rs, int64_t cs);
 template <typename T>
 int getrf_colmajor_host(luhot_ctx* ctx, int64_t m, int64_t n, T* a, int64_t rs, int64_t cs, uint64_t* piv,

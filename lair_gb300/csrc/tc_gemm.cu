@@ -2,7 +2,7 @@
 //
 //   C (M x N, FP32, row-major, ldc)  +=  alpha * A (M x K) * Bt (N x K)^T
 //
-// A and Bt are K-major operand copies in BF16, FP16 or FP32-read-as-TF32,
+// A and Bt are K-major operand copies in BF16, FP16 or TF32 (FP32 words rounded to TF32),
 // made per panel by tc_convert_kernel from the FP32 matrix being factored
 // (A = L21, Bt = U12^T), each scaled by a power of two so that its largest
 // magnitude sits at 2^14 (per-panel scaling: no FP16 overflow, few
@@ -660,7 +660,11 @@ __device__ __forceinline__ void store_op(void* dst, int64_t row, int k, int kall
     r[kalloc] = p1;
     r[2 * kalloc] = __float2bfloat16_rn(r2);
   } else {
-    reinterpret_cast<float*>(dst)[row * kalloc + k] = v;
+    // TF32: round to nearest here (the MMA would drop the low 13 bits), so
+    // the operand's unit roundoff is 2^-11, not 2^-10.
+    unsigned t;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(t) : "f"(v));
+    reinterpret_cast<unsigned*>(dst)[row * kalloc + k] = t;
   }
 }
 

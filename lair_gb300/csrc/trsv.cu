@@ -178,7 +178,9 @@ __global__ void __launch_bounds__(kThreads) trsv_syncfree_kernel(const TA* __res
   const int nupd = kLower ? I : (nblk - 1 - I);  // blocks before I in sweep order
   // Inverse of this block's diagonal tile (when given): fetched now, used last.
   T ireg[kPrefetch];
-  if (!kExact && dinv != nullptr) tile_load<T, T, false>(ireg, dinv + (int64_t)I * kBS * kBS, kBS, 0, 0, kBS, kBS);
+  // For op(A) = A^T the diagonal block of op(A) is the transpose of A's, and
+  // so is its inverse: the tile is read transposed.
+  if (!kExact && dinv != nullptr) tile_load<T, T, kTrans>(ireg, dinv + (int64_t)I * kBS * kBS, kBS, 0, 0, kBS, kBS);
   T reg[kPrefetch];
   if (nupd > 0) {
     const int J0 = kLower ? 0 : nblk - 1;
@@ -226,7 +228,7 @@ __global__ void __launch_bounds__(kThreads) trsv_syncfree_kernel(const TA* __res
     // Diagonal block by its precomputed inverse: x(I) = D^-1 xacc, a 64 x 64
     // matvec split like the updates (no sequential chain on the critical path).
     __syncthreads();
-    tile_store<T, false>(tile0, ireg);
+    tile_store<T, kTrans>(tile0, ireg);
 #pragma unroll
     for (int q = 0; q < kPP; ++q) {
       T v = acc[q];
@@ -376,7 +378,7 @@ cudaError_t launch_trsv_syncfree(cudaStream_t stream, const TA* a, int64_t lda, 
                                  DeviceStatus* st, const T* dinv) {
   if (n <= 0 || nrhs <= 0) return cudaSuccess;
   const int nblk = trsv_syncfree_blocks(n);
-  if (exact || trans) dinv = nullptr;  // inverses serve the fast untransposed sweeps only
+  if (exact) dinv = nullptr;  // inverses serve the fast sweeps only
   for (int c0 = 0; c0 < nrhs; c0 += kMaxRhs) {
     const int nc = std::min(kMaxRhs, nrhs - c0);
     cudaError_t e = cudaMemsetAsync(flags, 0, (size_t)nblk * sizeof(int), stream);

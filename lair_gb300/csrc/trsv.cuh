@@ -16,9 +16,10 @@ int trsv_syncfree_blocks(int n);
 // trsv_syncfree_blocks(n) ints and ticket one int of device scratch (both
 // cleared by this call); st supplies the wait limit and records a timeout.
 // TA is the storage type of the factor (it may be narrower than T).  dinv,
-// when not null, holds the inverses of the 64 x 64 diagonal blocks of this
-// triangle (launch_trsv_invert_diag) and replaces the sequential diagonal
-// solve by a matvec; it is ignored in exact mode and for transposed sweeps.
+// when not null, holds the inverses of the 64 x 64 diagonal blocks of the
+// triangle of A that the sweep reads (launch_trsv_invert_diag; for a
+// transposed sweep the inverses of A's blocks, read transposed) and replaces
+// the sequential diagonal solve by a matvec; it is ignored in exact mode.
 template <typename T, typename TA = T>
 cudaError_t launch_trsv_syncfree(cudaStream_t stream, const TA* a, int64_t lda, T* x, int64_t ldx, int n, int nrhs,
                                  bool lower, bool unit, bool trans, bool exact, int* flags, int* ticket,

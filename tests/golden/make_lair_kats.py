@@ -168,4 +168,6 @@ def main(root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_lair_kats.py /path/to/lair (the lair source tree)")
+    main(sys.argv[1])

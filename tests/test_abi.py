@@ -44,6 +44,26 @@ def test_ctypes_table_matches_header():
     assert set(_lib.SIGNATURES) == declared_functions()
 
 
+def declared_arity():
+    """Number of parameters of every function include/*.h declares."""
+    out = {}
+    for f in os.listdir(os.path.join(ROOT, "include")):
+        if f.endswith(".h"):
+            text = open(os.path.join(ROOT, "include", f)).read()
+            text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+            for name, params in re.findall(r"\b(luhot_\w+)\s*\(([^)]*)\)\s*;", text):
+                params = params.strip()
+                out[name] = 0 if params in ("", "void") else params.count(",") + 1
+    return out
+
+
+def test_ctypes_argument_counts_match_header():
+    arity = declared_arity()
+    assert set(arity) == declared_functions()
+    wrong = {n: (len(_lib.SIGNATURES[n][1]), arity[n]) for n in arity if len(_lib.SIGNATURES[n][1]) != arity[n]}
+    assert not wrong, f"ctypes argument count differs from the header (ctypes, header): {wrong}"
+
+
 def test_status_strings_without_gpu(lib):
     assert lib.luhot_status_string(0) == b"ok"
     assert lib.luhot_status_string(6) == b"matrix is singular"

@@ -90,3 +90,64 @@ def test_solve_with_fortran_factors_is_lairs():
     piv_r, _ = oracle.getrf(ref)
     x = lapack.getrs(gpu, piv, b, mode="exact")
     assert np.array_equal(x, oracle.getrs(ref, piv_r, b))
+
+
+def test_exact_nonstandard_beyond_4096_rows_is_unsupported():
+    """Exact mode never switches order: past 4096 rows a non-standard layout
+    is refused (LUHOT_ERR_UNSUPPORTED) on both the one-shot and the
+    device-resident paths."""
+    from lair_gb300 import _lib, lu
+
+    a = np.asfortranarray(rand(40, 4097, 6))
+    with pytest.raises(_lib.LuhotError) as e:
+        lapack.getrf(a.copy(order="F"), mode="exact")
+    assert e.value.status == _lib.LUHOT_ERR_UNSUPPORTED
+    with pytest.raises(_lib.LuhotError) as e:
+        lu.Factorized(a.copy(order="F"), mode="exact", device_resident=True)
+    assert e.value.status == _lib.LUHOT_ERR_UNSUPPORTED
+    piv, _ = lapack.getrf(a.copy(order="F"), mode="fast")  # fast mode takes it
+    assert len(piv) == 6
+
+
+@pytest.mark.parametrize("view", ["fortran", "reversed"])
+def test_resident_exact_nonstandard_is_lairs_bits(view):
+    from lair_gb300 import lu
+
+    n = 300
+    a0 = rand(41, n, n)
+    make = (lambda x: np.asfortranarray(x)) if view == "fortran" else (lambda x: x[::-1, ::-1])
+    ref = make(a0.copy())
+    piv_r, sing_r = oracle.getrf(ref)
+    f = lu.Factorized(make(a0.copy()), mode="exact", device_resident=True)
+    assert f.pivots == piv_r and f.singular == sing_r
+    assert np.array_equal(f.lu, ref)
+    b = rand(42, n, 1)[:, 0]
+    assert np.array_equal(f.solve(b), oracle.getrs(ref, piv_r, b))
+
+
+@pytest.mark.parametrize("view", ["fortran", "reversed", "padded_rows", "c_order"])
+def test_gesv_exact_follows_lairs_copy_layout(view):
+    """luhot_dgesv is equation::solve: lair factors a.to_owned(), which keeps
+    the strides of a contiguous array (F order, reversed) and makes any other
+    array standard; exact mode then gives the bits of lair's getrf on that
+    copy and its getrs (src/equation.rs:54-58)."""
+    from lair_gb300 import _lib
+    from lair_gb300.equation import _to_owned
+
+    n, nrhs = 150, 3
+    big = rand(43, n, n + 7)
+    views = {"fortran": lambda: np.asfortranarray(big[:, :n]), "reversed": lambda: big[:, :n].copy()[::-1, ::-1],
+             "padded_rows": lambda: big[:, :n], "c_order": lambda: big[:, :n].copy()}
+    a = views[view]()
+    b = rand(44, n, nrhs)
+    owned = _to_owned(a)
+    assert (view in ("fortran", "reversed")) == (not oracle.is_standard_layout(owned))
+    ref = owned.copy() if oracle.is_standard_layout(owned) else owned
+    piv_r, _ = oracle.getrf(ref)
+    x_ref = oracle.getrs_multi(ref, piv_r, b)
+    lib, ctx = _lib.load(), _lib.context()
+    x = np.empty((n, nrhs))
+    es = lambda v: tuple(s // v.itemsize for s in v.strides)  # noqa: E731
+    _lib.check(lib.luhot_dgesv(ctx, n, nrhs, a.ctypes.data, *es(a), b.ctypes.data, *es(b), x.ctypes.data, *es(x),
+                               _lib.MODE_EXACT), ctx)
+    assert np.array_equal(x, x_ref)
