@@ -14,6 +14,8 @@ Printed as one JSON line (rank 0):
             (luhot_dgesv: A, B copied in and X copied out every step)
   roofline  the Schur-update GEMM (the dominant kernel) against the FP64
             tensor-core peak measured in this run
+  resident_solve  lair's Factorized::solve with device-resident factors,
+            one right-hand side per call (the block-scaled sweeps)
   parity    pivots, ||PA - LU|| and the solution error against lair's
             results for the same inputs (tests/golden fixtures)
   cpu_baseline  lair's algorithm (the CPU oracle) on a bounded sample, plus
@@ -396,6 +398,10 @@ def run_ours(args):
                 "overall_frac_of_peak": (flops_of(n, nrhs) * args.steps / (ms_max * 1e-3) / 1e12) / peak
                 if peak else None}
 
+    resident = None
+    if not args.no_resident:
+        resident = run_resident_solve(args, lib, ctx, torch, A0, A, piv, peak)
+
     # e2e: equation::solve through the C ABI with host buffers every step
     e2e = None
     if not args.no_e2e:
@@ -460,7 +466,7 @@ def run_ours(args):
                 "berr_ok": berr <= n * EPS64, "parity": parity, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                 "clocks": clocks.summary(), "gpu_launches": int(launches),
                 "kernel_profile_ms": {k: round(v["ms"], 3) for k, v in prof.items()}, "ir": ir,
-                "batched": batched_res, "adjoint": adjoint_res, "qr": qr_res}
+                "resident_solve": resident, "batched": batched_res, "adjoint": adjoint_res, "qr": qr_res}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -582,6 +588,69 @@ def run_ir(args, lib, ctx, torch, rank):
             "fp64_backward_error": fp64_berr, "best": best, "best_gflops": results[best]["gflops"],
             "speedup_vs_fp64": fp64_ms / results[best]["ms"], "berr_bound": n * EPS64,
             "kappa_sweep": sweep}
+
+
+def run_resident_solve(args, lib, ctx, torch, A0, LU, piv, dmma_peak):
+    """lair's Factorized::solve with the factors kept on the device: one
+    right-hand side per call (luhot_dfactor_solve_dev), after a factor made
+    once from A (luhot_dfactor_create_dev).  The first solve forms the
+    block-scaled tiles; the next ones are timed one by one with CUDA events
+    (median).  Beside it, the plain sweeps on the same factors
+    (luhot_dgetrs_dev, one right-hand side).  Algorithmic bytes per solve:
+    both triangles of the factor read once, 8 n^2."""
+    import ctypes
+
+    from lair_gb300 import _lib
+
+    n = A0.shape[0]
+    stream = torch.cuda.current_stream()
+    h = ctypes.c_void_p()
+    pv = np.zeros(n, dtype=np.uint64)
+    sing = ctypes.c_int64(0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    _lib.check(lib.luhot_dfactor_create_dev(ctx, n, n, A0.data_ptr(), n, 0, pv.ctypes.data, ctypes.byref(sing),
+                                            ctypes.byref(h)), ctx)
+    create_s = time.perf_counter() - t0
+    gen = torch.Generator(device="cuda").manual_seed(77)
+    b0 = torch.randn(n, dtype=torch.float64, device="cuda", generator=gen)
+    xb = torch.empty_like(b0)
+
+    def timed(fn, reps):
+        ts = []
+        for _ in range(reps):
+            xb.copy_(b0)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return float(np.median(ts))
+
+    def resident():
+        _lib.check(lib.luhot_dfactor_solve_dev(h, 1, xb.data_ptr(), 1, 0), ctx)
+
+    def plain():
+        _lib.check(lib.luhot_dgetrs_dev(ctx, n, 1, LU.data_ptr(), n, piv.data_ptr(), xb.data_ptr(), 1, 0, 0), ctx)
+
+    first_ms = timed(resident, 1)  # forms W
+    ms = timed(resident, max(5, args.steps))
+    x = xb.clone()
+    berr = ((b0 - A0 @ x).abs().max() / (A0.abs().sum(1).max() * x.abs().max() + b0.abs().max())).item()
+    plain_ms = timed(plain, max(5, args.steps))
+    lib.luhot_factor_destroy(h)
+    byts = 8.0 * n * n
+    return {"workload": f"device-resident factors (Factorized::solve), n={n}, one right-hand side per call",
+            "factor_create_s": create_s, "first_solve_ms_forms_scaled_tiles": first_ms,
+            "ms_per_solve": ms, "ms_per_sweep": ms / 2, "backward_error": berr,
+            "achieved_gbs": byts / (ms * 1e-3) / 1e9,
+            "hbm_frac_of_measured": byts / (ms * 1e-3) / 1e9 / args.hbm_peak_gbs,
+            "fp64_floor_ms": 2.0 * n * n / (dmma_peak * 1e12) * 1e3,
+            "fp64_floor_note": "n^2 FMAs per solve at the measured FP64 peak: the arithmetic bound, above the HBM one",
+            "plain_sweeps_ms_per_solve": plain_ms,
+            "timing": "median of single solves, CUDA events; the factor exceeds L2"}
 
 
 def run_adjoint(args, lib, ctx, torch):
@@ -831,6 +900,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-qr", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-resident", action="store_true", help="skip the device-resident single-RHS solve leg")
     ap.add_argument("--adj-n", type=int, default=2048)
     ap.add_argument("--adj-nrhs", type=int, default=8)
     ap.add_argument("--hbm-peak-gbs", type=float, default=None,

@@ -11,6 +11,7 @@
 // what p()/l()/u() (lu.rs:28-72) need.
 #include <algorithm>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "common.cuh"
@@ -27,6 +28,11 @@ struct luhot_factor {
   int* d_perm = nullptr;  // m composed row order (m <= n only)
   void* d_dinv = nullptr; // inverses of the diagonal blocks of L then U (fast mode, m <= n)
   size_t dinv_elems = 0;  // per triangle
+  // Block-scaled off-diagonal tiles of L and U (FP64 fast mode, square),
+  // formed by the first single-right-hand-side solve; no_scaled once that
+  // allocation failed (later solves keep the plain sweeps).
+  double* d_w = nullptr;
+  bool no_scaled = false;
 };
 
 namespace luhot {
@@ -40,6 +46,7 @@ void free_factor(luhot_factor* f) {
   if (f->d_piv) cudaFree(f->d_piv);
   if (f->d_perm) cudaFree(f->d_perm);
   if (f->d_dinv) cudaFree(f->d_dinv);
+  if (f->d_w) cudaFree(f->d_w);
   delete f;
 }
 
@@ -171,6 +178,33 @@ int factor_solve(luhot_factor* f, int64_t nrhs, const T* b, int64_t b_rs, int64_
   if (rc) return rc;
   const T* dl = f->d_dinv ? static_cast<const T*>(f->d_dinv) : nullptr;
   const T* du = f->d_dinv ? dl + f->dinv_elems : nullptr;
+  if constexpr (std::is_same<T, double>::value) {
+    // One right-hand side, fast mode: the block-scaled sweeps (W formed once,
+    // n^2 more doubles on the device).
+    if (nrhs == 1 && !trans && dl && f->m == f->n && !f->no_scaled) {
+      if (!f->d_w) {
+        if (cudaMalloc(reinterpret_cast<void**>(&f->d_w), (size_t)n * f->lda * sizeof(double)) != cudaSuccess) {
+          cudaGetLastError();
+          f->d_w = nullptr;
+          f->no_scaled = true;
+        } else {
+          rc = scale_factor_blocks(ctx, (int)n, static_cast<const double*>(f->d_lu), f->lda, dl, du, f->d_w, f->lda);
+          if (rc) return rc;
+        }
+      }
+      if (f->d_w) {
+        rc = ensure_buf(ctx, ctx->work[3], 2 * (size_t)n * sizeof(double));
+        if (rc) return rc;
+        double* v1 = static_cast<double*>(ctx->work[3].ptr);
+        rc = getrs_scaled_apply(ctx, (int)n, f->d_w, f->lda, f->d_perm, d_b, ldb, d_b, ldb, dl, du, v1, v1 + n);
+        if (rc) return rc;
+        rc = finish_status(ctx, nullptr);
+        if (rc) return rc;
+        if (host) rc = stage_out<T>(ctx, d_b, ldb, x, n, nrhs, x_rs, x_cs, ctx->work[1]);
+        return rc;
+      }
+    }
+  }
   rc = getrs_apply<T>(ctx, (int)n, (int)nrhs, static_cast<const T*>(f->d_lu), f->lda, f->d_perm, d_b, ldb, d_b,
                       ldb, trans, f->mode, static_cast<T*>(ctx->work[3].ptr), dl, du);
   if (rc) return rc;

@@ -231,9 +231,11 @@ int trsv_scratch(luhot_ctx* ctx, int n, int** flags, int** ticket) {
   return LUHOT_OK;
 }
 
-template <typename T>
-int trsv_chain_sweep(luhot_ctx* ctx, const float* lu, int64_t lda, T* x, int n, bool lower, const T* dinv) {
-  const size_t words = trsv_chain_tag_words(n);
+// Tagged-word scratch of the chained and block-scaled sweeps (the context's
+// chain buffer: words, then the ticket) and a fresh epoch for one launch.  A
+// grown buffer is cleared, and so is every word when the 32-bit epoch wraps,
+// so no word ever carries the epoch of a later launch.
+static int sweep_tags(luhot_ctx* ctx, size_t words, unsigned long long** xt, int** ticket, unsigned int* epoch) {
   const size_t bytes = words * sizeof(unsigned long long) + 256;
   if (ctx->chain_buf.bytes < bytes) {
     int rc = ensure_buf(ctx, ctx->chain_buf, bytes);
@@ -241,15 +243,26 @@ int trsv_chain_sweep(luhot_ctx* ctx, const float* lu, int64_t lda, T* x, int n, 
     LUHOT_CUDA_TRY(ctx, cudaMemsetAsync(ctx->chain_buf.ptr, 0, ctx->chain_buf.bytes, ctx->stream));
     ctx->chain_epoch = 0;
   }
-  auto* xt = static_cast<unsigned long long*>(ctx->chain_buf.ptr);
-  int* ticket = reinterpret_cast<int*>(xt + words);
+  const size_t have = (ctx->chain_buf.bytes - 256) / sizeof(unsigned long long);
+  *xt = static_cast<unsigned long long*>(ctx->chain_buf.ptr);
+  *ticket = reinterpret_cast<int*>(*xt + have);
   if (++ctx->chain_epoch == 0) {  // the tag wrapped: clear every word once
-    LUHOT_CUDA_TRY(ctx, cudaMemsetAsync(xt, 0, words * sizeof(unsigned long long), ctx->stream));
+    LUHOT_CUDA_TRY(ctx, cudaMemsetAsync(*xt, 0, have * sizeof(unsigned long long), ctx->stream));
     ctx->chain_epoch = 1;
   }
+  *epoch = ctx->chain_epoch;
+  return LUHOT_OK;
+}
+
+template <typename T>
+int trsv_chain_sweep(luhot_ctx* ctx, const float* lu, int64_t lda, T* x, int n, bool lower, const T* dinv) {
+  unsigned long long* xt = nullptr;
+  int* ticket = nullptr;
+  unsigned int epoch = 0;
+  int rc = sweep_tags(ctx, trsv_chain_tag_words(n), &xt, &ticket, &epoch);
+  if (rc) return rc;
   prof_begin(ctx, kProfTrsv);
-  cudaError_t e = launch_trsv_chain<T>(ctx->stream, lu, lda, x, n, lower, dinv, xt, ctx->chain_epoch, ticket,
-                                       ctx->d_status);
+  cudaError_t e = launch_trsv_chain<T>(ctx->stream, lu, lda, x, n, lower, dinv, xt, epoch, ticket, ctx->d_status);
   prof_end(ctx, kProfTrsv, (double)n * n, (double)n * n / 2 * sizeof(float) + 2.0 * n * sizeof(T));
   count_launch(ctx);
   if (e != cudaSuccess) return set_error(ctx, LUHOT_ERR_CUDA, std::string("chained sweep: ") + cudaGetErrorString(e));
@@ -269,6 +282,43 @@ int chain_invert_blocks(luhot_ctx* ctx, int n, const float* lu, int64_t lda, T* 
 }
 
 template int trsv_chain_sweep<float>(luhot_ctx*, const float*, int64_t, float*, int, bool, const float*);
+
+int scale_factor_blocks(luhot_ctx* ctx, int n, const double* lu, int64_t lda, const double* dinv_l,
+                        const double* dinv_u, double* w, int64_t ldw) {
+  prof_begin(ctx, kProfTrsv);
+  cudaError_t e = launch_scale_blocks<double, double>(ctx->stream, lu, lda, dinv_l, dinv_u, w, ldw, n);
+  const double nblk = (n + 63) / 64;
+  prof_end(ctx, kProfTrsv, 2.0 * 64.0 * 64.0 * 64.0 * nblk * (nblk - 1), 3.0 * (double)n * n * sizeof(double));
+  count_launch(ctx);
+  if (e != cudaSuccess) return set_error(ctx, LUHOT_ERR_CUDA, std::string("block scaling: ") + cudaGetErrorString(e));
+  return LUHOT_OK;
+}
+
+int getrs_scaled_apply(luhot_ctx* ctx, int n, const double* w, int64_t ldw, const int* perm, const double* b,
+                       int64_t ldb, double* x, int64_t ldx, const double* dinv_l, const double* dinv_u, double* v1,
+                       double* v2) {
+  const int pblocks = (n + 255) / 256;
+  prof_begin(ctx, kProfPermute);
+  permute_rows_kernel<double, false><<<pblocks, 256, 0, ctx->stream>>>(b, ldb, v1, 1, perm, n, 1);
+  prof_end(ctx, kProfPermute, 0.0, 16.0 * n);
+  LUHOT_CUDA_TRY(ctx, cudaGetLastError());
+  for (int pass = 0; pass < 2; ++pass) {
+    unsigned long long* xt = nullptr;
+    int* ticket = nullptr;
+    unsigned int epoch = 0;
+    int rc = sweep_tags(ctx, trsv_scaled_tag_words(n), &xt, &ticket, &epoch);
+    if (rc) return rc;
+    const bool lower = pass == 0;
+    prof_begin(ctx, kProfTrsv);
+    cudaError_t e = launch_trsv_scaled<double>(ctx->stream, w, ldw, lower ? dinv_l : dinv_u, lower ? v1 : v2,
+                                               lower ? v2 : x, lower ? 1 : ldx, n, lower, xt, epoch, ticket,
+                                               ctx->d_status);
+    prof_end(ctx, kProfTrsv, (double)n * n, (double)n * n / 2 * sizeof(double) + 32.0 * n);
+    count_launch(ctx);
+    if (e != cudaSuccess) return set_error(ctx, LUHOT_ERR_CUDA, std::string("scaled sweep: ") + cudaGetErrorString(e));
+  }
+  return LUHOT_OK;
+}
 template int chain_invert_blocks<float>(luhot_ctx*, int, const float*, int64_t, float*, float*);
 
 template <typename T>

@@ -161,6 +161,16 @@ template <typename T>
 int getrs_apply(luhot_ctx* ctx, int n, int nrhs, const T* lu, int64_t lda, const int* perm, const T* b,
                 int64_t ldb, T* x, int64_t ldx, int trans, int mode, T* w, const T* dinv_l = nullptr,
                 const T* dinv_u = nullptr);
+// W = the block-scaled off-diagonal tiles of an n x n FP64 factor (see
+// launch_scale_blocks), and a single-right-hand-side solve with them:
+// x = U^-1 L^-1 P b, b and x strided (x may alias b), v1 and v2 n-vector
+// scratch.  Fast mode, untransposed; results agree with getrs_apply to
+// fast-mode rounding.
+int scale_factor_blocks(luhot_ctx* ctx, int n, const double* lu, int64_t lda, const double* dinv_l,
+                        const double* dinv_u, double* w, int64_t ldw);
+int getrs_scaled_apply(luhot_ctx* ctx, int n, const double* w, int64_t ldw, const int* perm, const double* b,
+                       int64_t ldb, double* x, int64_t ldx, const double* dinv_l, const double* dinv_u, double* v1,
+                       double* v2);
 // Inverses of the diagonal blocks of L (dinv_l) and U (dinv_u) of a
 // row-major LU factor; each holds trsv_inverse_elems(n) elements.  They let
 // the fast untransposed sweeps of getrs_apply replace each 64-step diagonal

@@ -25,6 +25,23 @@ cudaError_t launch_trsv_syncfree(cudaStream_t stream, const TA* a, int64_t lda, 
                                  bool lower, bool unit, bool trans, bool exact, int* flags, int* ticket,
                                  DeviceStatus* st, const T* dinv = nullptr);
 
+// Block-scaled single-right-hand-side sweeps (trsv_scaled.cu).  W holds,
+// for every off-diagonal 64 x 64 tile of L (below) and U (above) of an n x n
+// row-major factor, D_I^-1 T(I, J) with D_I the tile row's diagonal block;
+// launch_scale_blocks forms it from the factor and the diagonal inverses of
+// L and U.  launch_trsv_scaled then runs y = T^-1 b for the lower (L) or upper
+// (U) triangle with b contiguous and y strided (y must not alias b); xt is
+// tagged-word scratch of trsv_scaled_tag_words(n) words, epoch a tag no word
+// of xt holds yet, ticket one int (cleared by the call).
+size_t trsv_scaled_tag_words(int n);
+template <typename TA, typename TW>
+cudaError_t launch_scale_blocks(cudaStream_t stream, const TA* a, int64_t lda, const double* dinv_l,
+                                const double* dinv_u, TW* w, int64_t ldw, int n);
+template <typename TW>
+cudaError_t launch_trsv_scaled(cudaStream_t stream, const TW* w, int64_t ldw, const double* dinv, const double* b,
+                               double* y, int64_t ldy, int n, bool lower, unsigned long long* xt, unsigned int epoch,
+                               int* ticket, DeviceStatus* st);
+
 // Elements of the diagonal-block inverses for order n.
 size_t trsv_inverse_elems(int n);
 // Inverses of the diagonal blocks of the unit lower (lower) or non-unit upper

@@ -3,8 +3,10 @@
 The factor kept in HBM must give what the one-shot path gives on the same
 input: the same pivots, singular step and L\\U bits (the same getrf kernels),
 the same solutions bit for bit (the same sweeps with the same diagonal-block
-inverses), and in exact mode lair's bits (the oracle).  The host array must
-stay untouched until the factored array is first read.
+inverses; one FP64 right-hand side in fast mode takes the block-scaled sweeps
+instead and agrees to fast-mode rounding), and in exact mode lair's bits (the
+oracle).  The host array must stay untouched until the factored array is
+first read.
 """
 import ctypes
 
@@ -39,7 +41,13 @@ def test_resident_matches_one_shot_path_bitwise(n, dtype):
     assert np.array_equal(a, a0)  # nothing written back yet
     x = f.solve_matrix(b)
     assert np.array_equal(x, x_r)
-    assert np.array_equal(f.solve(b[:, 1]), lapack.getrs(ref, piv_r, b[:, 1]))
+    x1, x1_r = f.solve(b[:, 1]), lapack.getrs(ref, piv_r, b[:, 1])
+    if dtype == np.float64:
+        # one FP64 right-hand side takes the block-scaled sweeps: same
+        # solution to fast-mode rounding
+        np.testing.assert_allclose(x1, x1_r, rtol=0, atol=1e-9 * np.abs(x1_r).max())
+    else:
+        assert np.array_equal(x1, x1_r)
     assert np.array_equal(f.lu, ref)  # first read writes L\U into the caller's array
     assert f.lu is a
 
@@ -160,3 +168,23 @@ def test_resident_device_solve_and_status():
     _lib.check(lib.luhot_factor_device(h, ctypes.byref(ptr), ctypes.byref(lda), None), ctx)
     assert lda.value >= n and ptr.value
     lib.luhot_factor_destroy(h)
+
+
+@pytest.mark.parametrize("n", [1, 2, 63, 64, 65, 127, 129, 300, 1000, 2500])
+def test_resident_single_rhs_scaled_sweeps(n):
+    """One FP64 right-hand side (lair's Factorized::solve) runs the
+    block-scaled sweeps: W = D^-1 T formed at the first solve, then 64-row
+    blocks split over four CTAs.  Solutions must agree with the multi-RHS
+    sweeps to fast-mode rounding, meet the backward-error bound, and stay the
+    same on repeated solves (W is formed once)."""
+    a0 = np.random.default_rng(n + 90).standard_normal((n, n))
+    f = lu.Factorized(a0.copy(), device_resident=True)
+    rng = np.random.default_rng(n + 91)
+    for rep in range(3):
+        b = rng.standard_normal(n)
+        x = f.solve(b)
+        x2 = f.solve_matrix(np.stack([b, b], axis=1))[:, 0]  # the 64-row sync-free sweeps
+        np.testing.assert_allclose(x, x2, rtol=0, atol=1e-9 * np.abs(x2).max())
+        berr = np.abs(b - a0 @ x).max() / (np.abs(a0).sum(1).max() * np.abs(x).max() + np.abs(b).max())
+        assert berr <= max(n, 1) * EPS64, (rep, berr)
+        assert np.array_equal(f.solve(b), x)  # deterministic
