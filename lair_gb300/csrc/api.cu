@@ -506,6 +506,7 @@ void luhot_destroy(luhot_ctx* ctx) {
   if (ctx->tc_buf.ptr) cudaFree(ctx->tc_buf.ptr);
   if (ctx->dinv_buf.ptr) cudaFree(ctx->dinv_buf.ptr);
   if (ctx->chain_buf.ptr) cudaFree(ctx->chain_buf.ptr);
+  if (ctx->scaled_buf.ptr) cudaFree(ctx->scaled_buf.ptr);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
 }

@@ -1157,10 +1157,56 @@ static int launch_gemm(luhot_ctx* ctx, T* a, int64_t lda, int r0, int c0, int kk
   return LUHOT_OK;
 }
 
+// Row interchanges of the panel [k0, k0 + w) (the moves it reported) on every
+// column outside the panel: [0, k0) and [k0 + w, n).
+template <typename T>
+static int launch_laswp(luhot_ctx* ctx, T* a, int64_t lda, int k0, int w, int n, cudaStream_t stream) {
+  const int c_right = k0 + w;
+  const int ncols_swap = k0 + std::max(0, n - c_right);
+  if (ncols_swap <= 0) return LUHOT_OK;
+  prof_begin(ctx, kProfLaswp);
+  int* moves = reinterpret_cast<int*>(static_cast<char*>(ctx->panel_scratch) + kPanelSlotBytes);
+  const size_t lsm = (size_t)2 * w * 32 * sizeof(T);
+  LUHOT_CUDA_TRY(ctx, allow_max_dynamic_smem(laswp_moves_kernel<T>));
+  laswp_moves_kernel<T><<<(ncols_swap + 31) / 32, dim3(32, 8), lsm, stream>>>(
+      a, lda, moves, moves + 4 * kMaxPanelWidth, 2 * w, k0, c_right, n);
+  prof_end(ctx, kProfLaswp, 0.0, 4.0 * w * ncols_swap * sizeof(T));
+  LUHOT_CUDA_TRY(ctx, cudaGetLastError());
+  return LUHOT_OK;
+}
+
+// U12 = L11^-1 A12 for the panel [k0, k0 + w): rows [k0, k0 + w) of the
+// columns [c_begin, c_end).
 template <typename T, bool kExact>
-static int getrf_impl(luhot_ctx* ctx, int m, int n, T* a, int64_t lda, int* piv, int nb,
-                      cudaStream_t stream, int tc_kind = -1, void* tc_a = nullptr, void* tc_b = nullptr,
-                      float* tc_scal = nullptr) {
+static int launch_trsm(luhot_ctx* ctx, T* a, int64_t lda, int k0, int w, int c_begin, int c_end,
+                       cudaStream_t stream) {
+  if (c_begin >= c_end) return LUHOT_OK;
+  const int tgrid = (c_end - c_begin + kTrsmCols - 1) / kTrsmCols;
+  prof_begin(ctx, kProfTrsm);
+  if (!kExact && w <= 64) {
+    const size_t smem = ((size_t)64 * 64 + (size_t)64 * kTrsmCols) * sizeof(T);
+    LUHOT_CUDA_TRY(ctx, allow_max_dynamic_smem(trsm_fast_kernel<T, 64>));
+    trsm_fast_kernel<T, 64><<<tgrid, kTrsmCols, smem, stream>>>(a, lda, k0, w, c_begin, c_end);
+  } else if (!kExact && std::is_same<T, float>::value && w <= 128) {
+    if constexpr (std::is_same<T, float>::value) {
+      const size_t smem = ((size_t)128 * 128 + (size_t)128 * kTrsmCols) * sizeof(T);
+      LUHOT_CUDA_TRY(ctx, allow_max_dynamic_smem(trsm_fast_kernel<T, 128>));
+      trsm_fast_kernel<T, 128><<<tgrid, kTrsmCols, smem, stream>>>(a, lda, k0, w, c_begin, c_end);
+    }
+  } else {
+    const size_t smem = ((size_t)w * w + (size_t)w * kTrsmCols) * sizeof(T);
+    auto kern = trsm_kernel<T, kExact>;
+    LUHOT_CUDA_TRY(ctx, allow_max_dynamic_smem(kern));
+    kern<<<tgrid, kTrsmCols, smem, stream>>>(a, lda, k0, w, c_begin, c_end);
+  }
+  prof_end(ctx, kProfTrsm, (double)w * (w - 1) * (c_end - c_begin),
+           ((double)w * w + 2.0 * w * (c_end - c_begin)) * sizeof(T));
+  LUHOT_CUDA_TRY(ctx, cudaGetLastError());
+  return LUHOT_OK;
+}
+
+template <typename T, bool kExact>
+static int getrf_impl(luhot_ctx* ctx, int m, int n, T* a, int64_t lda, int* piv, int nb, cudaStream_t stream) {
   const int dim_min = std::min(m, n);
   // Exchange words carry step tags; clear them so no word of an earlier
   // factorization carries a live tag.
@@ -1168,52 +1214,56 @@ static int getrf_impl(luhot_ctx* ctx, int m, int n, T* a, int64_t lda, int* piv,
   for (int k0 = 0; k0 < dim_min; k0 += nb) {
     const int w = std::min(nb, dim_min - k0);
     int rc = launch_panel<T, kExact>(ctx, a, lda, m, k0, w, piv, stream);
-    if (rc != LUHOT_OK) return rc;
+    if (!rc) rc = launch_laswp<T>(ctx, a, lda, k0, w, n, stream);
+    if (rc) return rc;
     const int c_right = k0 + w;
-    const int ncols_swap = k0 + std::max(0, n - c_right);
-    if (ncols_swap > 0) {
-      prof_begin(ctx, kProfLaswp);
-      int* moves = reinterpret_cast<int*>(static_cast<char*>(ctx->panel_scratch) + kPanelSlotBytes);
-      const size_t lsm = (size_t)2 * w * 32 * sizeof(T);
-      LUHOT_CUDA_TRY(ctx, allow_max_dynamic_smem(laswp_moves_kernel<T>));
-      laswp_moves_kernel<T><<<(ncols_swap + 31) / 32, dim3(32, 8), lsm, stream>>>(
-          a, lda, moves, moves + 4 * kMaxPanelWidth, 2 * w, k0, c_right, n);
-      prof_end(ctx, kProfLaswp, 0.0, 4.0 * w * ncols_swap * sizeof(T));
-      LUHOT_CUDA_TRY(ctx, cudaGetLastError());
-    }
     if (c_right < n) {
-      const int tgrid = (n - c_right + kTrsmCols - 1) / kTrsmCols;
-      prof_begin(ctx, kProfTrsm);
-      if (!kExact && w <= 64) {
-        const size_t smem = ((size_t)64 * 64 + (size_t)64 * kTrsmCols) * sizeof(T);
-        LUHOT_CUDA_TRY(ctx, allow_max_dynamic_smem(trsm_fast_kernel<T, 64>));
-        trsm_fast_kernel<T, 64><<<tgrid, kTrsmCols, smem, stream>>>(a, lda, k0, w, c_right, n);
-      } else if (!kExact && std::is_same<T, float>::value && w <= 128) {
-        if constexpr (std::is_same<T, float>::value) {
-          const size_t smem = ((size_t)128 * 128 + (size_t)128 * kTrsmCols) * sizeof(T);
-          LUHOT_CUDA_TRY(ctx, allow_max_dynamic_smem(trsm_fast_kernel<T, 128>));
-          trsm_fast_kernel<T, 128><<<tgrid, kTrsmCols, smem, stream>>>(a, lda, k0, w, c_right, n);
-        }
-      } else {
-        const size_t smem = ((size_t)w * w + (size_t)w * kTrsmCols) * sizeof(T);
-        auto kern = trsm_kernel<T, kExact>;
-        LUHOT_CUDA_TRY(ctx, allow_max_dynamic_smem(kern));
-        kern<<<tgrid, kTrsmCols, smem, stream>>>(a, lda, k0, w, c_right, n);
-      }
-      prof_end(ctx, kProfTrsm, (double)w * (w - 1) * (n - c_right),
-               ((double)w * w + 2.0 * w * (n - c_right)) * sizeof(T));
-      LUHOT_CUDA_TRY(ctx, cudaGetLastError());
-      if constexpr (std::is_same<T, float>::value) {
-        if (tc_kind >= 0) {
-          rc = tc_schur_update(ctx, tc_kind, a, lda, k0, w, m, n, tc_a, tc_b, tc_scal, stream);
-          if (rc != LUHOT_OK) return rc;
-          continue;
-        }
-      }
-      rc = launch_gemm<T, kExact>(ctx, a, lda, k0 + w, c_right, k0, w, m - (k0 + w), n - c_right,
-                                  stream);
-      if (rc != LUHOT_OK) return rc;
+      rc = launch_trsm<T, kExact>(ctx, a, lda, k0, w, c_right, n, stream);
+      if (!rc) rc = launch_gemm<T, kExact>(ctx, a, lda, k0 + w, c_right, k0, w, m - (k0 + w), n - c_right, stream);
+      if (rc) return rc;
     }
+  }
+  return LUHOT_OK;
+}
+
+// The tensor-core factorization in slabs of two 128-column panels: the
+// trailing matrix is updated once per slab (K = 256), which halves its reads
+// and writes, the bound of that update.  Per slab [s0, s1):
+//   panel A = columns [s0, s0 + 128): factor, interchanges on the other columns;
+//   the slab's other half: its rows of U (trsm with A's L11), the rows below
+//     updated with K = 128, then panel B factored and its interchanges applied;
+//   the trailing columns: rows of U by two trsm steps with the update between
+//     them (the 256 x 256 unit lower L11 of the slab), then one update of the
+//     trailing block with K = 256 on the tensor cores.
+// The two K = 128 updates inside a slab (128 columns, or 128 rows) run as
+// FP32 CUDA-core GEMMs: one launch each, at least as accurate as any of the
+// tensor-core operand formats.
+static int getrf_tc_slabs(luhot_ctx* ctx, int m, int n, float* a, int64_t lda, int* piv, int tc_kind, void* tc_a,
+                          void* tc_b, float* tc_scal, cudaStream_t stream) {
+  const int dim_min = std::min(m, n);
+  LUHOT_CUDA_TRY(ctx, cudaMemsetAsync(ctx->panel_scratch, 0, kPanelScratchBytes, stream));
+  constexpr int hw = kTcPanelWidth;
+  for (int s0 = 0; s0 < dim_min; s0 += 2 * hw) {
+    const int sw = std::min(2 * hw, dim_min - s0);
+    const int h0 = std::min(hw, sw), h1 = sw - h0;
+    const int s1 = s0 + sw;
+    int rc = launch_panel<float, false>(ctx, a, lda, m, s0, h0, piv, stream);
+    if (!rc) rc = launch_laswp<float>(ctx, a, lda, s0, h0, n, stream);
+    if (!rc && h1 > 0) {
+      rc = launch_trsm<float, false>(ctx, a, lda, s0, h0, s0 + h0, s1, stream);
+      if (!rc) rc = launch_gemm<float, false>(ctx, a, lda, s0 + h0, s0 + h0, s0, h0, m - (s0 + h0), h1, stream);
+      if (!rc) rc = launch_panel<float, false>(ctx, a, lda, m, s0 + h0, h1, piv, stream);
+      if (!rc) rc = launch_laswp<float>(ctx, a, lda, s0 + h0, h1, n, stream);
+    }
+    if (!rc && s1 < n) {
+      rc = launch_trsm<float, false>(ctx, a, lda, s0, h0, s1, n, stream);
+      if (!rc && h1 > 0) {
+        rc = launch_gemm<float, false>(ctx, a, lda, s0 + h0, s1, s0, h0, h1, n - s1, stream);
+        if (!rc) rc = launch_trsm<float, false>(ctx, a, lda, s0 + h0, h1, s1, n, stream);
+      }
+      if (!rc) rc = tc_gemm_update(ctx, tc_kind, a, lda, s0, sw, s1, m, s1, n, tc_a, tc_b, tc_scal, stream);
+    }
+    if (rc) return rc;
   }
   return LUHOT_OK;
 }
@@ -1243,7 +1293,7 @@ int getrf_device_tc(luhot_ctx* ctx, int m, int n, float* a, int64_t lda, int* pi
   if (m < 0 || n < 0 || lda < std::max(1, n)) return set_error(ctx, LUHOT_ERR_INVALID_ARG, "getrf: bad shape or lda");
   if (singular) *singular = -1;
   if (m == 0 || n == 0) return LUHOT_OK;
-  const int nb = kTcPanelWidth;
+  const int nb = 2 * kTcPanelWidth;  // a slab's K
   const size_t bytes = tc_operand_bytes(tc_kind, m, nb) + tc_operand_bytes(tc_kind, n, nb) + 4096;
   int rc = ensure_buf(ctx, ctx->tc_buf, bytes);
   if (rc) return rc;
@@ -1253,7 +1303,7 @@ int getrf_device_tc(luhot_ctx* ctx, int m, int n, float* a, int64_t lda, int* pi
   float* tc_scal = reinterpret_cast<float*>(base + bytes - 1024);
   rc = reset_status(ctx);
   if (rc != LUHOT_OK) return rc;
-  rc = getrf_impl<float, false>(ctx, m, n, a, lda, piv, nb, ctx->stream, tc_kind, tc_a, tc_b, tc_scal);
+  rc = getrf_tc_slabs(ctx, m, n, a, lda, piv, tc_kind, tc_a, tc_b, tc_scal, ctx->stream);
   if (rc != LUHOT_OK) return rc;
   return finish_status(ctx, singular);
 }

@@ -283,16 +283,42 @@ int chain_invert_blocks(luhot_ctx* ctx, int n, const float* lu, int64_t lda, T* 
 
 template int trsv_chain_sweep<float>(luhot_ctx*, const float*, int64_t, float*, int, bool, const float*);
 
-int scale_factor_blocks(luhot_ctx* ctx, int n, const double* lu, int64_t lda, const double* dinv_l,
-                        const double* dinv_u, double* w, int64_t ldw) {
+template <typename T>
+int scale_factor_blocks(luhot_ctx* ctx, int n, const T* lu, int64_t lda, const double* dinv_l, const double* dinv_u,
+                        T* w, int64_t ldw) {
   prof_begin(ctx, kProfTrsv);
-  cudaError_t e = launch_scale_blocks<double, double>(ctx->stream, lu, lda, dinv_l, dinv_u, w, ldw, n);
+  cudaError_t e = launch_scale_blocks<T, T>(ctx->stream, lu, lda, dinv_l, dinv_u, w, ldw, n);
   const double nblk = (n + 63) / 64;
-  prof_end(ctx, kProfTrsv, 2.0 * 64.0 * 64.0 * 64.0 * nblk * (nblk - 1), 3.0 * (double)n * n * sizeof(double));
+  prof_end(ctx, kProfTrsv, 2.0 * 64.0 * 64.0 * 64.0 * nblk * (nblk - 1), 2.0 * (double)n * n * sizeof(T));
   count_launch(ctx);
   if (e != cudaSuccess) return set_error(ctx, LUHOT_ERR_CUDA, std::string("block scaling: ") + cudaGetErrorString(e));
   return LUHOT_OK;
 }
+template int scale_factor_blocks<double>(luhot_ctx*, int, const double*, int64_t, const double*, const double*,
+                                         double*, int64_t);
+template int scale_factor_blocks<float>(luhot_ctx*, int, const float*, int64_t, const double*, const double*, float*,
+                                        int64_t);
+
+template <typename TW>
+int scaled_sweep(luhot_ctx* ctx, const TW* w, int64_t ldw, const double* dinv, const double* b, double* y,
+                 int64_t ldy, int n, bool lower) {
+  unsigned long long* xt = nullptr;
+  int* ticket = nullptr;
+  unsigned int epoch = 0;
+  int rc = sweep_tags(ctx, trsv_scaled_tag_words(n), &xt, &ticket, &epoch);
+  if (rc) return rc;
+  prof_begin(ctx, kProfTrsv);
+  cudaError_t e = launch_trsv_scaled<TW>(ctx->stream, w, ldw, dinv, b, y, ldy, n, lower, xt, epoch, ticket,
+                                         ctx->d_status);
+  prof_end(ctx, kProfTrsv, (double)n * n, (double)n * n / 2 * sizeof(TW) + 32.0 * n);
+  count_launch(ctx);
+  if (e != cudaSuccess) return set_error(ctx, LUHOT_ERR_CUDA, std::string("scaled sweep: ") + cudaGetErrorString(e));
+  return LUHOT_OK;
+}
+template int scaled_sweep<double>(luhot_ctx*, const double*, int64_t, const double*, const double*, double*, int64_t,
+                                  int, bool);
+template int scaled_sweep<float>(luhot_ctx*, const float*, int64_t, const double*, const double*, double*, int64_t,
+                                 int, bool);
 
 int getrs_scaled_apply(luhot_ctx* ctx, int n, const double* w, int64_t ldw, const int* perm, const double* b,
                        int64_t ldb, double* x, int64_t ldx, const double* dinv_l, const double* dinv_u, double* v1,
@@ -302,22 +328,9 @@ int getrs_scaled_apply(luhot_ctx* ctx, int n, const double* w, int64_t ldw, cons
   permute_rows_kernel<double, false><<<pblocks, 256, 0, ctx->stream>>>(b, ldb, v1, 1, perm, n, 1);
   prof_end(ctx, kProfPermute, 0.0, 16.0 * n);
   LUHOT_CUDA_TRY(ctx, cudaGetLastError());
-  for (int pass = 0; pass < 2; ++pass) {
-    unsigned long long* xt = nullptr;
-    int* ticket = nullptr;
-    unsigned int epoch = 0;
-    int rc = sweep_tags(ctx, trsv_scaled_tag_words(n), &xt, &ticket, &epoch);
-    if (rc) return rc;
-    const bool lower = pass == 0;
-    prof_begin(ctx, kProfTrsv);
-    cudaError_t e = launch_trsv_scaled<double>(ctx->stream, w, ldw, lower ? dinv_l : dinv_u, lower ? v1 : v2,
-                                               lower ? v2 : x, lower ? 1 : ldx, n, lower, xt, epoch, ticket,
-                                               ctx->d_status);
-    prof_end(ctx, kProfTrsv, (double)n * n, (double)n * n / 2 * sizeof(double) + 32.0 * n);
-    count_launch(ctx);
-    if (e != cudaSuccess) return set_error(ctx, LUHOT_ERR_CUDA, std::string("scaled sweep: ") + cudaGetErrorString(e));
-  }
-  return LUHOT_OK;
+  int rc = scaled_sweep<double>(ctx, w, ldw, dinv_l, v1, v2, 1, n, true);
+  if (!rc) rc = scaled_sweep<double>(ctx, w, ldw, dinv_u, v2, x, ldx, n, false);
+  return rc;
 }
 template int chain_invert_blocks<float>(luhot_ctx*, int, const float*, int64_t, float*, float*);
 

@@ -221,6 +221,9 @@ namespace {
 // about 250 at n = 16384; restarting every 120 iterations stalled there.
 constexpr int kGmresRestart = 400;
 constexpr double kGmresTol = 1e-6;  // relative reduction of the preconditioned residual per solve
+// Preconditioner applications in one solve before the block-scaled tiles are
+// formed: the forming costs about as much as 24 plain applications at large n.
+constexpr int kScaledAfter = 24;
 
 // Device scalars.
 enum Sc : int { kAnorm = 0, kBnorm, kRnorm, kXnorm, kVscale, kNrm2, kH = 8 };
@@ -240,6 +243,9 @@ struct IrRun {
   Tlo* lo2;
   double* r;   // residual / Arnoldi work
   double* t;   // second FP64 work vector
+  double* u;   // third FP64 work vector (block-scaled preconditioner sweeps)
+  float* w32 = nullptr;  // block-scaled tiles of the factors, once formed
+  int minv_calls = 0;    // preconditioner applications of this solve
   double* V;   // (restart + 1) x n
   double* sc;  // device scalars
   double* hsc; // pinned host mirror of sc
@@ -273,6 +279,29 @@ struct IrRun {
   // FP64 arithmetic is slow on this part, so these sweeps keep 64-row
   // blocks (a quarter of the per-step FP64 work of the chained 128-row form).
   int lo_solve64(const double* v, double* out) {
+    // After kScaledAfter applications (a long GMRES run), the block-scaled
+    // tiles of the factors are formed once (in FP64 arithmetic, stored in
+    // FP32) and every later application uses the block-scaled sweeps, whose
+    // critical path per 64-row block is a quarter of the FMAs.
+    if (!w32 && ++minv_calls > kScaledAfter && n > 64) {
+      if (ensure_buf(ctx, ctx->scaled_buf, (size_t)n * ldlo * sizeof(float)) == LUHOT_OK) {
+        float* w = static_cast<float*>(ctx->scaled_buf.ptr);
+        int rc = scale_factor_blocks<float>(ctx, n, lu, ldlo, dl64, du64, w, ldlo);
+        if (rc) return rc;
+        w32 = w;
+      } else {
+        ctx->last_error.clear();  // no room: keep the plain sweeps
+        minv_calls = INT32_MIN;
+      }
+    }
+    if (w32) {
+      prof_begin(ctx, kProfRefine);
+      ir_gather_kernel<double><<<grid_vec, 256, 0, ctx->stream>>>(v, perm, out, n);
+      prof_end(ctx, kProfRefine, 0.0, 20.0 * n);
+      int rc = scaled_sweep<float>(ctx, w32, ldlo, dl64, out, u, 1, n, true);
+      if (!rc) rc = scaled_sweep<float>(ctx, w32, ldlo, du64, u, out, 1, n, false);
+      return rc;
+    }
     int* flags = nullptr;
     int* ticket = nullptr;
     int rc = trsv_scratch(ctx, n, &flags, &ticket);
@@ -436,7 +465,7 @@ static int ir_setup(luhot_ctx* ctx, int n, const double* a, int64_t lda, IrRun<f
   int rc = ensure_buf(ctx, ctx->ir_buf[0], (size_t)n * ldlo * sizeof(float));
   if (rc) return rc;
   const size_t vecs = (size_t)n * sizeof(double);
-  rc = ensure_buf(ctx, ctx->ir_buf[1], vecs * (2 + kGmresRestart + 1) + 3 * (size_t)n * sizeof(float) + 4096);
+  rc = ensure_buf(ctx, ctx->ir_buf[1], vecs * (3 + kGmresRestart + 1) + 3 * (size_t)n * sizeof(float) + 4096);
   if (rc) return rc;
   const size_t idx_ints = (2 * (size_t)n + 63) / 64 * 64;  // pivots + permutation, 256-byte aligned end
   rc = ensure_buf(ctx, ctx->ir_buf[2], idx_ints * sizeof(int) + kIrScalarSlots * sizeof(double));
@@ -450,7 +479,8 @@ static int ir_setup(luhot_ctx* ctx, int n, const double* a, int64_t lda, IrRun<f
   char* base = static_cast<char*>(ctx->ir_buf[1].ptr);
   s.r = reinterpret_cast<double*>(base);
   s.t = s.r + n;
-  s.V = s.t + n;
+  s.u = s.t + n;
+  s.V = s.u + n;
   s.lo1 = reinterpret_cast<float*>(s.V + (size_t)(kGmresRestart + 1) * n);
   s.lo2 = s.lo1 + n;
   s.piv = static_cast<int*>(ctx->ir_buf[2].ptr);

@@ -84,6 +84,7 @@ struct luhot_ctx {
   luhot::DevBuf tc_buf;                     // tensor-core LU: operand copies + scales
   luhot::DevBuf dinv_buf;                   // inverses of the 64 x 64 diagonal blocks of L and U
   luhot::DevBuf chain_buf;                  // chained sweeps: tagged x words + ticket
+  luhot::DevBuf scaled_buf;                 // GMRES-IR: block-scaled tiles of the FP32 factor
   unsigned int chain_epoch = 0;             // tag of the last chained sweep (0 = none)
   double* h_scalars = nullptr;              // pinned: scalars read back by the refinement loop
   void* h_piv = nullptr;                    // pinned pivots staging
@@ -166,8 +167,16 @@ int getrs_apply(luhot_ctx* ctx, int n, int nrhs, const T* lu, int64_t lda, const
 // x = U^-1 L^-1 P b, b and x strided (x may alias b), v1 and v2 n-vector
 // scratch.  Fast mode, untransposed; results agree with getrs_apply to
 // fast-mode rounding.
-int scale_factor_blocks(luhot_ctx* ctx, int n, const double* lu, int64_t lda, const double* dinv_l,
-                        const double* dinv_u, double* w, int64_t ldw);
+// (T = float: tiles of an FP32 factor, formed in FP64 arithmetic and stored
+// in FP32, for the FP64-arithmetic preconditioner of GMRES-IR.)
+template <typename T>
+int scale_factor_blocks(luhot_ctx* ctx, int n, const T* lu, int64_t lda, const double* dinv_l, const double* dinv_u,
+                        T* w, int64_t ldw);
+// One block-scaled sweep y = T^-1 b (b contiguous, y with stride ldy, y not
+// aliasing b) on the context's stream with fresh tagged-word scratch.
+template <typename TW>
+int scaled_sweep(luhot_ctx* ctx, const TW* w, int64_t ldw, const double* dinv, const double* b, double* y,
+                 int64_t ldy, int n, bool lower);
 int getrs_scaled_apply(luhot_ctx* ctx, int n, const double* w, int64_t ldw, const int* perm, const double* b,
                        int64_t ldb, double* x, int64_t ldx, const double* dinv_l, const double* dinv_u, double* v1,
                        double* v2);

@@ -772,13 +772,24 @@ static int make_c_map(luhot_ctx* ctx, CUtensorMap* m, float* c, int M, int N, in
   return LUHOT_OK;
 }
 
+// a[r1.., c1..] (M = m - r1 rows, N = n - c1 columns) -= a[r1.., k0..k0+w] a[k0..k0+w, c1..]
 template <int KIND>
-static int launch_tc(luhot_ctx* ctx, float* a, int64_t lda, int k0, int w, int m, int n, void* aop, void* bop,
-                     float* scal, cudaStream_t stream) {
-  const int r1 = k0 + w, c1 = k0 + w;
+static int launch_tc(luhot_ctx* ctx, float* a, int64_t lda, int k0, int w, int r1, int m, int c1, int n, void* aop,
+                     void* bop, float* scal, cudaStream_t stream) {
   const int M = m - r1, N = n - c1;
-  if (M <= 0 || N <= 0) return LUHOT_OK;
+  if (M <= 0 || N <= 0 || w <= 0) return LUHOT_OK;
   const int kalloc = tc_kalloc(KIND, w);
+  {
+    // The one-tile fallback (unaligned C) stages all of K in shared memory:
+    // past 128 it takes the update in two halves.
+    float* cb = a + (int64_t)r1 * lda + c1;
+    const bool aligned = (lda % 4 == 0) && (reinterpret_cast<uintptr_t>(cb) % 16 == 0);
+    if (!(aligned && TcShape<KIND>::kSmem <= (size_t)ctx->max_smem_optin) && w > 128) {
+      int rc = launch_tc<KIND>(ctx, a, lda, k0, 128, r1, m, c1, n, aop, bop, scal, stream);
+      if (rc) return rc;
+      return launch_tc<KIND>(ctx, a, lda, k0 + 128, w - 128, r1, m, c1, n, aop, bop, scal, stream);
+    }
+  }
   // scales
   LUHOT_CUDA_TRY(ctx, cudaMemsetAsync(scal, 0, 8 * sizeof(float), stream));
   prof_begin(ctx, kProfGemm);
@@ -825,15 +836,20 @@ static int launch_tc(luhot_ctx* ctx, float* a, int64_t lda, int k0, int w, int m
   return LUHOT_OK;
 }
 
-int tc_schur_update(luhot_ctx* ctx, int kind, float* a, int64_t lda, int k0, int w, int m, int n, void* aop, void* bop,
-                    float* scal, cudaStream_t stream) {
+int tc_gemm_update(luhot_ctx* ctx, int kind, float* a, int64_t lda, int k0, int w, int r1, int m, int c1, int n,
+                   void* aop, void* bop, float* scal, cudaStream_t stream) {
   switch (kind) {
-    case kTcBF16: return launch_tc<kTcBF16>(ctx, a, lda, k0, w, m, n, aop, bop, scal, stream);
-    case kTcFP16: return launch_tc<kTcFP16>(ctx, a, lda, k0, w, m, n, aop, bop, scal, stream);
-    case kTcTF32: return launch_tc<kTcTF32>(ctx, a, lda, k0, w, m, n, aop, bop, scal, stream);
-    case kTcBF16x3: return launch_tc<kTcBF16x3>(ctx, a, lda, k0, w, m, n, aop, bop, scal, stream);
+    case kTcBF16: return launch_tc<kTcBF16>(ctx, a, lda, k0, w, r1, m, c1, n, aop, bop, scal, stream);
+    case kTcFP16: return launch_tc<kTcFP16>(ctx, a, lda, k0, w, r1, m, c1, n, aop, bop, scal, stream);
+    case kTcTF32: return launch_tc<kTcTF32>(ctx, a, lda, k0, w, r1, m, c1, n, aop, bop, scal, stream);
+    case kTcBF16x3: return launch_tc<kTcBF16x3>(ctx, a, lda, k0, w, r1, m, c1, n, aop, bop, scal, stream);
     default: return set_error(ctx, LUHOT_ERR_INVALID_ARG, "unknown tensor-core operand kind");
   }
+}
+
+int tc_schur_update(luhot_ctx* ctx, int kind, float* a, int64_t lda, int k0, int w, int m, int n, void* aop, void* bop,
+                    float* scal, cudaStream_t stream) {
+  return tc_gemm_update(ctx, kind, a, lda, k0, w, k0 + w, m, k0 + w, n, aop, bop, scal, stream);
 }
 
 }  // namespace luhot

@@ -21,5 +21,9 @@ size_t tc_operand_bytes(int kind, int rows, int w);
 // bop: tc_operand_bytes(kind, m or n, w) each) and 8 floats of scalars.
 int tc_schur_update(luhot_ctx* ctx, int kind, float* a, int64_t lda, int k0, int w, int m, int n, void* aop,
                     void* bop, float* scal, cudaStream_t stream);
+// The same on any block: a[r1..m, c1..n] -= a[r1..m, k0..k0+w] a[k0..k0+w, c1..n]
+// (the operand copies must hold tc_operand_bytes(kind, m - r1 or n - c1, w)).
+int tc_gemm_update(luhot_ctx* ctx, int kind, float* a, int64_t lda, int k0, int w, int r1, int m, int c1, int n,
+                   void* aop, void* bop, float* scal, cudaStream_t stream);
 
 }  // namespace luhot

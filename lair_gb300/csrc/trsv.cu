@@ -392,9 +392,9 @@ cudaError_t launch_trsv_syncfree(cudaStream_t stream, const TA* a, int64_t lda, 
     else if (!exact && !lower && !unit && !trans)
       e = launch_case<T, TA, false, false, false, false>(stream, a, lda, xc, ldx, n, nc, flags, ticket, st, dinv);
     else if (!exact && lower && !unit && trans)
-      e = launch_case<T, TA, false, true, false, true>(stream, a, lda, xc, ldx, n, nc, flags, ticket, st, nullptr);
+      e = launch_case<T, TA, false, true, false, true>(stream, a, lda, xc, ldx, n, nc, flags, ticket, st, dinv);
     else if (!exact && !lower && unit && trans)
-      e = launch_case<T, TA, false, false, true, true>(stream, a, lda, xc, ldx, n, nc, flags, ticket, st, nullptr);
+      e = launch_case<T, TA, false, false, true, true>(stream, a, lda, xc, ldx, n, nc, flags, ticket, st, dinv);
     else
       return cudaErrorNotSupported;
     if (e != cudaSuccess) return e;

@@ -18,8 +18,8 @@
 // take (block, quarter) tickets in sweep order and wait only for blocks of
 // earlier tickets, i.e. of CTAs already running; x(I) is published as
 // epoch-tagged words (two per FP64 value, each carrying the launch's epoch in
-// its top half), and every thread polls exactly the eight values it needs
-// with 32-byte loads, so the loop has no flags, fences or block barriers.
+// its top half), which each warp polls with one 32-byte load per lane and a
+// vote, so the loop has no flags, fences or block barriers.
 // Thread layout: 128 threads = 16 rows x 8 groups of 8 columns; each thread
 // keeps one partial sum, reduced over the 8 lanes of its row once at the end.
 // Every wait is bounded by the context's wait limit (LUHOT_ERR_TIMEOUT).
@@ -93,22 +93,60 @@ __device__ __forceinline__ void scaled_st_word(unsigned long long* p, unsigned i
   asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
-// Eight consecutive entries of row i of W from column j (zero past n).
-template <typename TW>
-__device__ __forceinline__ void scaled_load_row8(double (&d)[8], const TW* __restrict__ w, int64_t ldw, int i, int j,
-                                                 int n) {
-  const TW* src = w + (int64_t)i * ldw + j;
+// Eight consecutive entries of row i of W from column j (zero past n); the
+// whole-segment case as 16-byte loads (j is a multiple of 8 and rows start
+// on 256-byte boundaries).
+__device__ __forceinline__ void scaled_load_row8(double (&d)[8], const double* __restrict__ w, int64_t ldw, int i,
+                                                 int j, int n) {
+  const double* src = w + (int64_t)i * ldw + j;
   if (i < n && j + 8 <= n) {
 #pragma unroll
-    for (int e = 0; e < 8; ++e) d[e] = static_cast<double>(__ldg(src + e));
+    for (int q = 0; q < 4; ++q) {
+      const double2 v = __ldg(reinterpret_cast<const double2*>(src) + q);
+      d[2 * q] = v.x;
+      d[2 * q + 1] = v.y;
+    }
+  } else {
+#pragma unroll
+    for (int e = 0; e < 8; ++e) d[e] = (i < n && j + e < n) ? __ldg(src + e) : 0.0;
+  }
+}
+__device__ __forceinline__ void scaled_load_row8(double (&d)[8], const float* __restrict__ w, int64_t ldw, int i,
+                                                 int j, int n) {
+  const float* src = w + (int64_t)i * ldw + j;
+  if (i < n && j + 8 <= n) {
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const float4 v = __ldg(reinterpret_cast<const float4*>(src) + q);
+      d[4 * q] = v.x;
+      d[4 * q + 1] = v.y;
+      d[4 * q + 2] = v.z;
+      d[4 * q + 3] = v.w;
+    }
   } else {
 #pragma unroll
     for (int e = 0; e < 8; ++e) d[e] = (i < n && j + e < n) ? static_cast<double>(__ldg(src + e)) : 0.0;
   }
 }
 
+// Whether a lane's quad of tagged words (values 2L and 2L + 1 of a block of
+// `count` published values) carries this launch's epoch.
+__device__ __forceinline__ bool scaled_quad_ok(const unsigned long long (&q)[4], int lane, int count,
+                                               unsigned int epoch) {
+  const bool v0 = 2 * lane >= count || ((unsigned int)(q[0] >> 32) == epoch && (unsigned int)(q[1] >> 32) == epoch);
+  const bool v1 = 2 * lane + 1 >= count || ((unsigned int)(q[2] >> 32) == epoch && (unsigned int)(q[3] >> 32) == epoch);
+  return v0 && v1;
+}
+__device__ __forceinline__ double scaled_decode(unsigned long long hi, unsigned long long lo) {
+  return __longlong_as_double((long long)(((unsigned long long)(unsigned int)hi << 32) | (unsigned int)lo));
+}
+
 // One sweep: y = T^-1 b (b and y are n-vectors with strides 1 and ldy; y may
 // not alias b).  xt holds two tagged words per row (at least 2 * 64 * nblk).
+// x(J) is fetched per warp: lane L loads the 32-byte quad of values 2L and
+// 2L + 1, the warp votes on the tags, the values go through a per-warp
+// shared buffer to the eight lanes of each row that use them; the next
+// tile's quad is requested while the current tile is used.
 template <typename TW, bool kLower>
 __global__ void __launch_bounds__(kSThreads) trsv_scaled_kernel(const TW* __restrict__ w, int64_t ldw,
                                                                 const double* __restrict__ dinv,
@@ -116,6 +154,7 @@ __global__ void __launch_bounds__(kSThreads) trsv_scaled_kernel(const TW* __rest
                                                                 int n, unsigned long long* xt, unsigned int epoch,
                                                                 int* ticket, DeviceStatus* st) {
   __shared__ int s_ticket;
+  __shared__ double s_x[kSThreads / 32][2][kSB];
   if (threadIdx.x == 0) s_ticket = atomicAdd(ticket, 1);
   __syncthreads();
   const int nblk = (n + kSB - 1) / kSB;
@@ -123,6 +162,7 @@ __global__ void __launch_bounds__(kSThreads) trsv_scaled_kernel(const TW* __rest
   if (t >= nblk * kSParts) return;
   const int I = kLower ? t / kSParts : nblk - 1 - t / kSParts;
   const int part = t % kSParts;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int r = threadIdx.x >> 3, kp = threadIdx.x & 7;
   const int rb = part * kSRows + r;  // row within the block
   const int i = I * kSB + rb;        // this thread's row
@@ -140,60 +180,61 @@ __global__ void __launch_bounds__(kSThreads) trsv_scaled_kernel(const TW* __rest
 
   const int nupd = kLower ? I : nblk - 1 - I;
   double cur[8], nxt[8];
-  if (nupd > 0) scaled_load_row8(nxt, w, ldw, i, (kLower ? 0 : nblk - 1) * kSB + c8, n);
+  unsigned long long q[4];
+  if (nupd > 0) {
+    const int J0 = kLower ? 0 : nblk - 1;
+    scaled_load_row8(nxt, w, ldw, i, J0 * kSB + c8, n);
+    scaled_ld_quad(xt + 2 * (size_t)J0 * kSB + 4 * lane, q);
+  }
   const unsigned long long limit = st->timeout_ns;
-  // A wait that gives up (or sees another's abort) ends this thread's loop;
-  // every lane still reaches the warp's shuffles below.
+  // Every branch below is warp-uniform (votes and shuffles), so a wait that
+  // gives up ends the loop for the whole warp and every lane still reaches
+  // the shuffles after it.
   bool alive = true;
-  for (int s = 0; s < nupd && alive; ++s) {
+  for (int s = 0; s < nupd; ++s) {
     const int J = kLower ? s : nblk - 1 - s;
-    const int j = J * kSB + c8;
+    const int j0 = J * kSB;
+    const int count = min(kSB, n - j0);
 #pragma unroll
     for (int e = 0; e < 8; ++e) cur[e] = nxt[e];
     if (s + 1 < nupd) scaled_load_row8(nxt, w, ldw, i, (kLower ? s + 1 : nblk - 2 - s) * kSB + c8, n);
-    const int valid = max(0, min(8, n - j));  // published values among this thread's eight
-    if (valid == 0) continue;
-    unsigned long long wd[16];
-    const unsigned long long* src = xt + 2 * (size_t)j;
     unsigned long long t0 = 0;
     unsigned int spins = 0;
-    for (;;) {
-#pragma unroll
-      for (int q = 0; q < 4; ++q) scaled_ld_quad(src + 4 * q, wd + 4 * q);
-      bool ok = true;
-#pragma unroll
-      for (int e = 0; e < 16; ++e) ok = ok && ((e >> 1) >= valid || (unsigned int)(wd[e] >> 32) == epoch);
-      if (ok) break;
+    while (!__all_sync(0xffffffffu, scaled_quad_ok(q, lane, count, epoch))) {
       if (spins == 0) t0 = global_timer_ns();
       if ((++spins & 63u) == 0) {
-        if (ld_relaxed_i32(&st->abort)) {
-          alive = false;
-          break;
+        int stop = 0;
+        if (lane == 0) {
+          if (ld_relaxed_i32(&st->abort)) {
+            stop = 1;
+          } else if (global_timer_ns() - t0 > limit) {
+            atomicCAS(&st->error, kDevOk, kDevBarrierTimeout);
+            atomicExch(&st->timeout_where, (unsigned long long)J);
+            atomicExch(&st->abort, 1);
+            stop = 1;
+          }
         }
-        if (global_timer_ns() - t0 > limit) {
-          atomicCAS(&st->error, kDevOk, kDevBarrierTimeout);
-          atomicExch(&st->timeout_where, (unsigned long long)J);
-          atomicExch(&st->abort, 1);
+        if (__shfl_sync(0xffffffffu, stop, 0)) {
           alive = false;
           break;
         }
       }
+      scaled_ld_quad(xt + 2 * (size_t)j0 + 4 * lane, q);
     }
     if (!alive) break;
+    double* xb = s_x[warp][s & 1];
+    xb[2 * lane] = 2 * lane < count ? scaled_decode(q[0], q[1]) : 0.0;
+    xb[2 * lane + 1] = 2 * lane + 1 < count ? scaled_decode(q[2], q[3]) : 0.0;
+    if (s + 1 < nupd) scaled_ld_quad(xt + 2 * (size_t)(kLower ? s + 1 : nblk - 2 - s) * kSB + 4 * lane, q);
+    __syncwarp();
 #pragma unroll
-    for (int e = 0; e < 8; ++e) {
-      const double xv = e < valid ? __longlong_as_double((long long)(((unsigned long long)(unsigned int)wd[2 * e] << 32) |
-                                                                     (unsigned int)wd[2 * e + 1]))
-                                  : 0.0;
-      acc = fma(-cur[e], xv, acc);
-    }
+    for (int e = 0; e < 8; ++e) acc = fma(-cur[e], xb[c8 + e], acc);
   }
   // Sum the row's eight partial sums (lanes 8r' .. 8r'+7 of the warp).
   acc += __shfl_xor_sync(0xffffffffu, acc, 1);
   acc += __shfl_xor_sync(0xffffffffu, acc, 2);
   acc += __shfl_xor_sync(0xffffffffu, acc, 4);
-  const bool publish = __all_sync(0xffffffffu, alive);
-  if (publish && kp == 0 && i < n) {
+  if (alive && kp == 0 && i < n) {
     y[(int64_t)i * ldy] = acc;
     const unsigned long long bits = (unsigned long long)__double_as_longlong(acc);
     scaled_st_word(xt + 2 * (size_t)i, (unsigned int)(bits >> 32), epoch);
@@ -235,6 +276,11 @@ cudaError_t launch_trsv_scaled(cudaStream_t stream, const TW* w, int64_t ldw, co
 
 template cudaError_t launch_scale_blocks<double, double>(cudaStream_t, const double*, int64_t, const double*,
                                                          const double*, double*, int64_t, int);
+template cudaError_t launch_scale_blocks<float, float>(cudaStream_t, const float*, int64_t, const double*,
+                                                       const double*, float*, int64_t, int);
+template cudaError_t launch_trsv_scaled<float>(cudaStream_t, const float*, int64_t, const double*, const double*,
+                                               double*, int64_t, int, bool, unsigned long long*, unsigned int, int*,
+                                               DeviceStatus*);
 template cudaError_t launch_trsv_scaled<double>(cudaStream_t, const double*, int64_t, const double*, const double*,
                                                 double*, int64_t, int, bool, unsigned long long*, unsigned int, int*,
                                                 DeviceStatus*);
