@@ -12,8 +12,15 @@ Printed as one JSON line (rank 0):
   value     device-resident throughput (inputs in HBM when timing starts)
   e2e       the same solve through the C ABI with host buffers
             (luhot_dgesv: A, B copied in and X copied out every step)
-  roofline  the Schur-update GEMM (the dominant kernel) against the FP64
-            tensor-core peak measured in this run
+  roofline  the Schur update (the dominant kernel).  With the default engine
+            (--fp64-update auto) the large updates run on the FP16 tensor cores
+            as exact integer-slice products (34 slice GEMMs per update): the
+            executed FP16 work against the measured tensor peak, with the
+            FP64-equivalent rate and C's HBM traffic beside it.  With
+            --fp64-update dmma: against the FP64 tensor-core peak measured
+            in this run.
+  fp64_update  the engine, and one step timed with the DMMA engine for
+            comparison
   resident_solve  lair's Factorized::solve with device-resident factors,
             one right-hand side per call (the block-scaled sweeps)
   parity    pivots, ||PA - LU|| and the solution error against lair's
@@ -214,20 +221,36 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+OZ_PRODUCTS = 34  # FP16 slice GEMMs per tensor-core FP64 update (groups p + q <= 7 of 7 x 7)
+
+
 def workload_config(args):
     return {"workload": f"plain FP64 getrf+getrs drop-in, n={args.n}, nrhs={args.nrhs}, A,B iid N(0,1) seeded "
                         "(portable generator, lair_gb300.synthetic)",
             "n": args.n, "nrhs": args.nrhs, "mode": args.mode,
+            "fp64_update": {"auto": "FP16 tensor cores, exact integer slices (Ozaki), on trailing blocks >= 256 x 256; "
+                                    "DMMA below",
+                            "dmma": "FP64 tensor cores (DMMA) only",
+                            "ozaki": "FP16 tensor cores, exact integer slices, on every block >= 128 x 64"}[
+                                        args.fp64_update],
             "l2": "inputs larger than L2 (A is %.1f GiB vs 129 MB L2)" % (args.n * args.n * 8 / 2 ** 30),
             "parallelism": "replicas (one independent system per GPU)"}
+
+
+def measured_peaks() -> dict:
+    """The measured peaks of the GB300s (empty if absent)."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
 
 
 def measured_hbm_peak() -> float:
     """HBM copy bandwidth measured on the GB300s, else the fallback."""
     try:
-        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-            return float(json.load(f)["hbm_gbs"])
-    except (OSError, ValueError, KeyError):
+        return float(measured_peaks()["hbm_gbs"])
+    except (KeyError, TypeError, ValueError):
         return 6800.0
 
 
@@ -312,6 +335,7 @@ def run_ours(args):
     torch.cuda.set_stream(stream)
     _lib.check(lib.luhot_set_stream(ctx, ctypes.c_void_p(stream.cuda_stream)), ctx)
     mode = _lib.mode_id(args.mode)
+    _lib.check(lib.luhot_set_fp64_update(ctx, _lib.FP64_UPDATES[args.fp64_update]), ctx)
 
     n, nrhs = args.n, args.nrhs
     lda = n
@@ -384,19 +408,63 @@ def run_ours(args):
         parity = parity_vs_lair(torch, n, fixture, A0, A, piv, X) if inputs_match else {
             "error": "inputs were not reproduced bit for bit; no comparison"}
 
-    g = prof.get("gemm", {"ms": 0.0, "flops": 0.0, "launches": 0})
+    g = prof.get("gemm", {"ms": 0.0, "flops": 0.0, "bytes": 0.0, "launches": 0})
     gemm_tflops = g["flops"] / (g["ms"] * 1e-3) / 1e12 if g["ms"] else 0.0
-    traffic = read_traffic(os.path.join(ROOT, "profiles", "gemm_dmma_persistent_fp64_n16384.md"))
     total_prof_ms = sum(v["ms"] for v in prof.values())
-    roofline = {"bound": "tensor", "achieved": gemm_tflops, "peak": peak, "unit": "TFLOP/s",
-                "frac": gemm_tflops / peak if peak else None, "traffic": traffic,
-                "kernel": "gemm_dmma_persistent_kernel (FP64 Schur update, mma.sync m8n8k4)",
-                "peak_source": "FP64 DMMA throughput measured in this run (register-resident "
-                               "mma.sync m8n8k4 loop); MEASURED_PEAKS.json has no FP64 figure",
-                "per_launch_flops": g["flops"] / max(1, g["launches"]),
-                "launches": g["launches"], "share_of_step": g["ms"] / total_prof_ms if total_prof_ms else None,
-                "overall_frac_of_peak": (flops_of(n, nrhs) * args.steps / (ms_max * 1e-3) / 1e12) / peak
-                if peak else None}
+    share = g["ms"] / total_prof_ms if total_prof_ms else None
+    overall = flops_of(n, nrhs) * args.steps / (ms_max * 1e-3) / 1e12
+    sliced = args.fp64_update != "dmma" and prof.get("other", {}).get("launches", 0) > 0
+    if sliced:
+        # Every large update is 34 FP16 slice GEMMs of the same shape (the
+        # few small trailing blocks on DMMA are a negligible share).
+        tensor_peak = measured_peaks().get("bf16_tflops_sustained", 1700.0)
+        executed = OZ_PRODUCTS * gemm_tflops
+        c_gbs = g["bytes"] / (g["ms"] * 1e-3) / 1e9 if g["ms"] else 0.0
+        roofline = {"bound": "tensor", "achieved": executed, "peak": tensor_peak, "unit": "TFLOP/s",
+                    "frac": executed / tensor_peak,
+                    "traffic": read_traffic(os.path.join(ROOT, "profiles", "oz_gemm_fp64_slices_n16384.md")),
+                    "kernel": "oz_gemm_kernel (FP64 Schur update as 34 exact FP16 slice GEMMs, tcgen05 + TMA)",
+                    "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (dense FP16 = BF16 rate; the "
+                                   "kernel runs inside a seconds-long step)",
+                    "achieved_is": "executed FP16 tensor work: 34 slice products x 2MNK per launch / event time",
+                    "fp64_equivalent_tflops": gemm_tflops,
+                    "fp64_equivalent_vs_dmma_peak": gemm_tflops / peak if peak else None,
+                    "hbm": {"achieved_gbs": c_gbs, "peak_gbs": args.hbm_peak_gbs,
+                            "frac": c_gbs / args.hbm_peak_gbs,
+                            "bytes_are": "C read + written once per update, the slices read once"},
+                    "per_launch_fp64_flops": g["flops"] / max(1, g["launches"]),
+                    "launches": g["launches"], "share_of_step": share,
+                    "split_ms": prof["other"]["ms"] / args.steps,
+                    "overall_fp64_tflops": overall}
+    else:
+        traffic = read_traffic(os.path.join(ROOT, "profiles", "gemm_dmma_persistent_fp64_n16384.md"))
+        roofline = {"bound": "tensor", "achieved": gemm_tflops, "peak": peak, "unit": "TFLOP/s",
+                    "frac": gemm_tflops / peak if peak else None, "traffic": traffic,
+                    "kernel": "gemm_dmma_persistent_kernel (FP64 Schur update, mma.sync m8n8k4)",
+                    "peak_source": "FP64 DMMA throughput measured in this run (register-resident "
+                                   "mma.sync m8n8k4 loop); MEASURED_PEAKS.json has no FP64 figure",
+                    "per_launch_flops": g["flops"] / max(1, g["launches"]),
+                    "launches": g["launches"], "share_of_step": share,
+                    "overall_frac_of_peak": overall / peak if peak else None}
+
+    engine_cmp = {"engine": args.fp64_update}
+    if args.fp64_update != "dmma" and not args.no_dmma_step:
+        # one step with the FP64-tensor-core engine, for comparison
+        _lib.check(lib.luhot_set_fp64_update(ctx, _lib.UPDATE_DMMA), ctx)
+        step()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        _lib.check(lib.luhot_set_fp64_update(ctx, _lib.FP64_UPDATES[args.fp64_update]), ctx)
+        dmma_ms = e0.elapsed_time(e1)
+        engine_cmp.update({"dmma_ms_per_step": dmma_ms, "speedup_vs_dmma": dmma_ms / (ms_max / args.steps),
+                           "dmma_gflops": flops_of(n, nrhs) / (dmma_ms * 1e-3) / 1e9})
+        step()  # leave the factors of the default engine for the legs below
+        torch.cuda.synchronize()
 
     resident = None
     if not args.no_resident:
@@ -465,7 +533,8 @@ def run_ours(args):
                 "config": workload_config(args), "backward_error": berr, "berr_bound": n * EPS64,
                 "berr_ok": berr <= n * EPS64, "parity": parity, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                 "clocks": clocks.summary(), "gpu_launches": int(launches),
-                "kernel_profile_ms": {k: round(v["ms"], 3) for k, v in prof.items()}, "ir": ir,
+                "kernel_profile_ms": {k: round(v["ms"], 3) for k, v in prof.items()}, "fp64_update": engine_cmp,
+                "ir": ir,
                 "resident_solve": resident, "batched": batched_res, "adjoint": adjoint_res, "qr": qr_res}
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -889,6 +958,9 @@ def main():
     ap.add_argument("--n", type=int, default=16384)
     ap.add_argument("--nrhs", type=int, default=16)
     ap.add_argument("--mode", choices=["fast", "exact"], default="fast")
+    ap.add_argument("--fp64-update", choices=["auto", "dmma", "ozaki"], default="auto",
+                    help="Schur-update engine of fast-mode FP64 getrf")
+    ap.add_argument("--no-dmma-step", action="store_true", help="skip the one comparison step with DMMA")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")

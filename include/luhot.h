@@ -71,6 +71,24 @@ const char* luhot_last_error(const luhot_ctx* ctx);
 int luhot_set_stream(luhot_ctx* ctx, void* cuda_stream);
 /* Panel width override (0 = default 64); for tuning and tests. */
 int luhot_set_block(luhot_ctx* ctx, int nb);
+/* Schur-update engine of fast-mode FP64 getrf (no lair counterpart).
+ * LUHOT_UPDATE_AUTO (default): trailing blocks of at least 256 x 256 are
+ * updated on the FP16 tensor cores by an exact integer-slice product (Ozaki
+ * scheme: seven 8-bit slices per operand, 34 slice products, FP32 sums that
+ * are exact, one FP64 rounding; error at or below an FP64 GEMM's), smaller
+ * ones on the FP64 tensor cores (DMMA).  LUHOT_UPDATE_DMMA: DMMA only.
+ * LUHOT_UPDATE_OZAKI: the tensor-core product on every block of at least
+ * 128 x 64.  Exact mode and FP32 ignore the setting. */
+#define LUHOT_UPDATE_AUTO 0
+#define LUHOT_UPDATE_DMMA 1
+#define LUHOT_UPDATE_OZAKI 2
+int luhot_set_fp64_update(luhot_ctx* ctx, int engine);
+/* One trailing update of fast-mode FP64 getrf on its own (no lair
+ * counterpart): for the row-major m x n FP64 device matrix d_a (lda),
+ *   d_a[k.., k..] -= d_a[k.., 0..k) d_a[0..k), k..],   1 <= k <= 64,
+ * with the given LUHOT_UPDATE_* engine (AUTO chooses by size as getrf does).
+ * For callers that block their own factorizations, and for tests. */
+int luhot_dschur_update_dev(luhot_ctx* ctx, int64_t m, int64_t n, int64_t k, double* d_a, int64_t lda, int engine);
 /* Kernel launches issued by this context since creation. */
 int64_t luhot_launch_count(const luhot_ctx* ctx);
 /* Self-test of the device-side wait limit: launches two CTAs that wait on a
@@ -81,8 +99,9 @@ int luhot_selftest_wait_timeout(luhot_ctx* ctx, int64_t timeout_ms);
 
 /* Per-kernel-class CUDA-event profile (no lair counterpart).  Classes:
  * 0 panel, 1 laswp, 2 trsm, 3 Schur GEMM, 4 triangular solve (getrs),
- * 5 permutation, 6 refinement (residual / update), 7 other.  flops and
- * bytes are the algorithmic work of the timed launches. */
+ * 5 permutation, 6 refinement (residual / update), 7 other (in getrf: the
+ * operand splits of the tensor-core FP64 update).  flops and bytes are the
+ * algorithmic work of the timed launches. */
 typedef struct luhot_profile {
   double ms[8];
   double flops[8];

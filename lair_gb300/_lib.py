@@ -42,6 +42,8 @@ SIGNATURES = {
     "luhot_set_stream": (_i32, [_vp, _vp]),
     "luhot_set_block": (_i32, [_vp, _i32]),
     "luhot_launch_count": (_i64, [_vp]),
+    "luhot_set_fp64_update": (_i32, [_vp, _i32]),
+    "luhot_dschur_update_dev": (_i32, [_vp, _i64, _i64, _i64, _vp, _i64, _i32]),
     "luhot_selftest_wait_timeout": (_i32, [_vp, _i64]),
     "luhot_profile_enable": (_i32, [_vp, _i32]),
     "luhot_profile_read": (_i32, [_vp, _vp]),
@@ -105,6 +107,8 @@ class Profile(ctypes.Structure):
                 for i, name in enumerate(PROFILE_CLASSES) if self.launches[i]}
 
 
+UPDATE_AUTO, UPDATE_DMMA, UPDATE_OZAKI = 0, 1, 2
+FP64_UPDATES = {"auto": UPDATE_AUTO, "dmma": UPDATE_DMMA, "ozaki": UPDATE_OZAKI}
 PREC_FP32, PREC_BF16, PREC_FP16, PREC_TF32, PREC_BF16X3 = 0, 1, 2, 3, 4
 PRECISIONS = {"fp32": PREC_FP32, "bf16": PREC_BF16, "fp16": PREC_FP16, "tf32": PREC_TF32, "bf16x3": PREC_BF16X3}
 REFINE_IR, REFINE_GMRES = 0, 1
@@ -187,6 +191,14 @@ def profile_read() -> dict:
     prof = Profile()
     check(load().luhot_profile_read(ctx, ctypes.byref(prof)), ctx)
     return prof.as_dict()
+
+
+def set_fp64_update(engine) -> None:
+    """Schur-update engine of fast-mode FP64 getrf: "auto" (tensor-core FP64 by
+    integer slices on large blocks, DMMA on small ones), "dmma" or "ozaki"."""
+    ctx = context()
+    eid = engine if isinstance(engine, int) else FP64_UPDATES[engine]
+    check(load().luhot_set_fp64_update(ctx, eid), ctx)
 
 
 def dmma_peak_tflops() -> float:

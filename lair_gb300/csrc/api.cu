@@ -507,6 +507,7 @@ void luhot_destroy(luhot_ctx* ctx) {
   if (ctx->dinv_buf.ptr) cudaFree(ctx->dinv_buf.ptr);
   if (ctx->chain_buf.ptr) cudaFree(ctx->chain_buf.ptr);
   if (ctx->scaled_buf.ptr) cudaFree(ctx->scaled_buf.ptr);
+  if (ctx->oz_buf.ptr) cudaFree(ctx->oz_buf.ptr);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
 }
@@ -525,6 +526,29 @@ int luhot_set_block(luhot_ctx* ctx, int nb) {
   Guard g(ctx);
   ctx->nb_override = nb;
   return LUHOT_OK;
+}
+
+int luhot_set_fp64_update(luhot_ctx* ctx, int engine) {
+  if (!ctx || engine < LUHOT_UPDATE_AUTO || engine > LUHOT_UPDATE_OZAKI) return LUHOT_ERR_INVALID_ARG;
+  Guard g(ctx);
+  ctx->fp64_update = engine;
+  return LUHOT_OK;
+}
+
+int luhot_dschur_update_dev(luhot_ctx* ctx, int64_t m, int64_t n, int64_t k, double* d_a, int64_t lda, int engine) {
+  LUHOT_NVTX_FN();
+  if (!ctx) return LUHOT_ERR_INVALID_ARG;
+  Guard g(ctx);
+  if (!dims_ok(m, n) || k < 1 || k > kDefaultPanelWidth || k > std::min(m, n) || lda < std::max<int64_t>(1, n))
+    return set_error(ctx, LUHOT_ERR_INVALID_ARG, "schur update: invalid dimensions");
+  if (engine < LUHOT_UPDATE_AUTO || engine > LUHOT_UPDATE_OZAKI)
+    return set_error(ctx, LUHOT_ERR_INVALID_ARG, "schur update: unknown engine");
+  if (!d_a) return set_error(ctx, LUHOT_ERR_INVALID_ARG, "schur update: null pointer");
+  int rc = reset_status(ctx);
+  if (rc) return rc;
+  rc = fp64_schur_update(ctx, d_a, lda, (int)k, (int)m, (int)n, engine);
+  if (rc) return rc;
+  return finish_status(ctx, nullptr);
 }
 
 int64_t luhot_launch_count(const luhot_ctx* ctx) { return ctx ? ctx->launches.load() : 0; }

@@ -32,6 +32,7 @@
 
 #include "common.cuh"
 #include "luhot_internal.h"
+#include "ozaki.cuh"
 #include "tc_gemm.cuh"
 
 namespace luhot {
@@ -1205,8 +1206,44 @@ static int launch_trsm(luhot_ctx* ctx, T* a, int64_t lda, int k0, int w, int c_b
   return LUHOT_OK;
 }
 
+// The trailing update of the panel [k0, k0 + w): a[r1.., r1..] -= L21 U12,
+// r1 = k0 + w.  Fast-mode FP64 runs it on the FP16 tensor cores (ozaki.cu)
+// when a workspace was given and the block is large enough for the engine
+// setting, else on the FP64 tensor cores.
 template <typename T, bool kExact>
-static int getrf_impl(luhot_ctx* ctx, int m, int n, T* a, int64_t lda, int* piv, int nb, cudaStream_t stream) {
+static int schur_update(luhot_ctx* ctx, T* a, int64_t lda, int k0, int w, int m, int n, void* oz_ws, int engine,
+                        cudaStream_t stream) {
+  const int r1 = k0 + w;
+  if constexpr (std::is_same<T, double>::value && !kExact) {
+    const int M = m - r1, N = n - r1;
+    const bool big = engine == LUHOT_UPDATE_OZAKI ? (M >= 128 && N >= 64) : (M >= 256 && N >= 256);
+    if (oz_ws && engine != LUHOT_UPDATE_DMMA && big)
+      return ozaki_update(ctx, a, lda, k0, w, r1, m, r1, n, oz_ws, stream);
+  }
+  return launch_gemm<T, kExact>(ctx, a, lda, r1, r1, k0, w, m - r1, n - r1, stream);
+}
+
+// Workspace of the tensor-core FP64 update for an m x n factorization
+// (nullptr: the engine setting or the device rules it out).
+static int ozaki_workspace(luhot_ctx* ctx, int m, int n, int engine, void** ws) {
+  *ws = nullptr;
+  if (engine == LUHOT_UPDATE_DMMA || !ozaki_available(ctx)) return LUHOT_OK;
+  int rc = ensure_buf(ctx, ctx->oz_buf, ozaki_workspace_bytes(m, n));
+  if (rc != LUHOT_OK) return rc;
+  *ws = ctx->oz_buf.ptr;
+  return LUHOT_OK;
+}
+
+int fp64_schur_update(luhot_ctx* ctx, double* a, int64_t lda, int k, int m, int n, int engine) {
+  void* ws = nullptr;
+  int rc = ozaki_workspace(ctx, m, n, engine, &ws);
+  if (rc) return rc;
+  return schur_update<double, false>(ctx, a, lda, 0, k, m, n, ws, engine, ctx->stream);
+}
+
+template <typename T, bool kExact>
+static int getrf_impl(luhot_ctx* ctx, int m, int n, T* a, int64_t lda, int* piv, int nb, void* oz_ws,
+                      cudaStream_t stream) {
   const int dim_min = std::min(m, n);
   // Exchange words carry step tags; clear them so no word of an earlier
   // factorization carries a live tag.
@@ -1219,7 +1256,7 @@ static int getrf_impl(luhot_ctx* ctx, int m, int n, T* a, int64_t lda, int* piv,
     const int c_right = k0 + w;
     if (c_right < n) {
       rc = launch_trsm<T, kExact>(ctx, a, lda, k0, w, c_right, n, stream);
-      if (!rc) rc = launch_gemm<T, kExact>(ctx, a, lda, k0 + w, c_right, k0, w, m - (k0 + w), n - c_right, stream);
+      if (!rc) rc = schur_update<T, kExact>(ctx, a, lda, k0, w, m, n, oz_ws, ctx->fp64_update, stream);
       if (rc) return rc;
     }
   }
@@ -1278,10 +1315,15 @@ int getrf_device(luhot_ctx* ctx, int m, int n, T* a, int64_t lda, int* piv, int 
   int rc = reset_status(ctx);
   if (rc != LUHOT_OK) return rc;
   const int nb = ctx->nb_override > 0 ? std::min(ctx->nb_override, kDefaultPanelWidth) : kDefaultPanelWidth;
+  void* oz_ws = nullptr;
+  if (std::is_same<T, double>::value && mode != LUHOT_MODE_EXACT) {
+    rc = ozaki_workspace(ctx, m, n, ctx->fp64_update, &oz_ws);
+    if (rc != LUHOT_OK) return rc;
+  }
   if (mode == LUHOT_MODE_EXACT)
-    rc = getrf_impl<T, true>(ctx, m, n, a, lda, piv, nb, stream);
+    rc = getrf_impl<T, true>(ctx, m, n, a, lda, piv, nb, nullptr, stream);
   else
-    rc = getrf_impl<T, false>(ctx, m, n, a, lda, piv, nb, stream);
+    rc = getrf_impl<T, false>(ctx, m, n, a, lda, piv, nb, oz_ws, stream);
   if (rc != LUHOT_OK) return rc;
   return finish_status(ctx, singular);
 }

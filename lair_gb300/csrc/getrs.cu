@@ -283,21 +283,22 @@ int chain_invert_blocks(luhot_ctx* ctx, int n, const float* lu, int64_t lda, T* 
 
 template int trsv_chain_sweep<float>(luhot_ctx*, const float*, int64_t, float*, int, bool, const float*);
 
-template <typename T>
-int scale_factor_blocks(luhot_ctx* ctx, int n, const T* lu, int64_t lda, const double* dinv_l, const double* dinv_u,
-                        T* w, int64_t ldw) {
+template <typename TA, typename TW>
+int scale_factor_blocks(luhot_ctx* ctx, int n, const TA* lu, int64_t lda, const double* dinv_l, const double* dinv_u,
+                        TW* w, int64_t ldw) {
   prof_begin(ctx, kProfTrsv);
-  cudaError_t e = launch_scale_blocks<T, T>(ctx->stream, lu, lda, dinv_l, dinv_u, w, ldw, n);
+  cudaError_t e = launch_scale_blocks<TA, TW>(ctx->stream, lu, lda, dinv_l, dinv_u, w, ldw, n);
   const double nblk = (n + 63) / 64;
-  prof_end(ctx, kProfTrsv, 2.0 * 64.0 * 64.0 * 64.0 * nblk * (nblk - 1), 2.0 * (double)n * n * sizeof(T));
+  prof_end(ctx, kProfTrsv, 2.0 * 64.0 * 64.0 * 64.0 * nblk * (nblk - 1),
+           (double)n * n * (sizeof(TA) + sizeof(TW)));
   count_launch(ctx);
   if (e != cudaSuccess) return set_error(ctx, LUHOT_ERR_CUDA, std::string("block scaling: ") + cudaGetErrorString(e));
   return LUHOT_OK;
 }
-template int scale_factor_blocks<double>(luhot_ctx*, int, const double*, int64_t, const double*, const double*,
-                                         double*, int64_t);
-template int scale_factor_blocks<float>(luhot_ctx*, int, const float*, int64_t, const double*, const double*, float*,
-                                        int64_t);
+template int scale_factor_blocks<double, double>(luhot_ctx*, int, const double*, int64_t, const double*,
+                                                 const double*, double*, int64_t);
+template int scale_factor_blocks<float, double>(luhot_ctx*, int, const float*, int64_t, const double*, const double*,
+                                                double*, int64_t);
 
 template <typename TW>
 int scaled_sweep(luhot_ctx* ctx, const TW* w, int64_t ldw, const double* dinv, const double* b, double* y,
@@ -317,8 +318,6 @@ int scaled_sweep(luhot_ctx* ctx, const TW* w, int64_t ldw, const double* dinv, c
 }
 template int scaled_sweep<double>(luhot_ctx*, const double*, int64_t, const double*, const double*, double*, int64_t,
                                   int, bool);
-template int scaled_sweep<float>(luhot_ctx*, const float*, int64_t, const double*, const double*, double*, int64_t,
-                                 int, bool);
 
 int getrs_scaled_apply(luhot_ctx* ctx, int n, const double* w, int64_t ldw, const int* perm, const double* b,
                        int64_t ldb, double* x, int64_t ldx, const double* dinv_l, const double* dinv_u, double* v1,

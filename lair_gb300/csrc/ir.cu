@@ -244,7 +244,7 @@ struct IrRun {
   double* r;   // residual / Arnoldi work
   double* t;   // second FP64 work vector
   double* u;   // third FP64 work vector (block-scaled preconditioner sweeps)
-  float* w32 = nullptr;  // block-scaled tiles of the factors, once formed
+  double* w64 = nullptr; // block-scaled tiles of the factors, once formed
   int minv_calls = 0;    // preconditioner applications of this solve
   double* V;   // (restart + 1) x n
   double* sc;  // device scalars
@@ -280,26 +280,30 @@ struct IrRun {
   // blocks (a quarter of the per-step FP64 work of the chained 128-row form).
   int lo_solve64(const double* v, double* out) {
     // After kScaledAfter applications (a long GMRES run), the block-scaled
-    // tiles of the factors are formed once (in FP64 arithmetic, stored in
-    // FP32) and every later application uses the block-scaled sweeps, whose
-    // critical path per 64-row block is a quarter of the FMAs.
-    if (!w32 && ++minv_calls > kScaledAfter && n > 64) {
-      if (ensure_buf(ctx, ctx->scaled_buf, (size_t)n * ldlo * sizeof(float)) == LUHOT_OK) {
-        float* w = static_cast<float*>(ctx->scaled_buf.ptr);
-        int rc = scale_factor_blocks<float>(ctx, n, lu, ldlo, dl64, du64, w, ldlo);
+    // tiles of the factors are formed once, in FP64 arithmetic and FP64
+    // storage, and every later application uses the block-scaled sweeps,
+    // whose critical path per 64-row block is a quarter of the FMAs.  The
+    // tiles stay in FP64: rounding W = D^-1 T to FP32 perturbs the applied
+    // factor by up to 2^-24 cond(D) relative, and on the weak (TF32, FP16,
+    // BF16) factors, whose GMRES runs take hundreds of iterations, that
+    // perturbation cost up to twice the iterations.
+    if (!w64 && ++minv_calls > kScaledAfter && n > 64) {
+      if (ensure_buf(ctx, ctx->scaled_buf, (size_t)n * ldlo * sizeof(double)) == LUHOT_OK) {
+        double* w = static_cast<double*>(ctx->scaled_buf.ptr);
+        int rc = scale_factor_blocks(ctx, n, lu, ldlo, dl64, du64, w, ldlo);
         if (rc) return rc;
-        w32 = w;
+        w64 = w;
       } else {
         ctx->last_error.clear();  // no room: keep the plain sweeps
         minv_calls = INT32_MIN;
       }
     }
-    if (w32) {
+    if (w64) {
       prof_begin(ctx, kProfRefine);
       ir_gather_kernel<double><<<grid_vec, 256, 0, ctx->stream>>>(v, perm, out, n);
       prof_end(ctx, kProfRefine, 0.0, 20.0 * n);
-      int rc = scaled_sweep<float>(ctx, w32, ldlo, dl64, out, u, 1, n, true);
-      if (!rc) rc = scaled_sweep<float>(ctx, w32, ldlo, du64, u, out, 1, n, false);
+      int rc = scaled_sweep<double>(ctx, w64, ldlo, dl64, out, u, 1, n, true);
+      if (!rc) rc = scaled_sweep<double>(ctx, w64, ldlo, du64, u, out, 1, n, false);
       return rc;
     }
     int* flags = nullptr;

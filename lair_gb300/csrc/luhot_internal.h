@@ -85,11 +85,13 @@ struct luhot_ctx {
   luhot::DevBuf dinv_buf;                   // inverses of the 64 x 64 diagonal blocks of L and U
   luhot::DevBuf chain_buf;                  // chained sweeps: tagged x words + ticket
   luhot::DevBuf scaled_buf;                 // GMRES-IR: block-scaled tiles of the FP32 factor
+  luhot::DevBuf oz_buf;                     // FP64 getrf: digit slices of the tensor-core update
   unsigned int chain_epoch = 0;             // tag of the last chained sweep (0 = none)
   double* h_scalars = nullptr;              // pinned: scalars read back by the refinement loop
   void* h_piv = nullptr;                    // pinned pivots staging
   size_t h_piv_bytes = 0;
   int nb_override = 0;
+  int fp64_update = LUHOT_UPDATE_AUTO;  // Schur-update engine of fast-mode FP64 getrf
   bool trace = false;  // LUHOT_TRACE=1: refinement steps are reported on stderr
   unsigned long long wait_timeout_ns = 2000000000ull;  // per device-side wait
   std::atomic<int64_t> launches{0};
@@ -115,6 +117,9 @@ int copy_2d(luhot_ctx* ctx, void* dst, size_t dpitch, const void* src, size_t sp
 template <typename T>
 int getrf_device(luhot_ctx* ctx, int m, int n, T* a, int64_t lda, int* piv, int mode,
                  int64_t* singular);
+// One fast-mode FP64 trailing update, a[k.., k..] -= a[k.., 0..k) a[0..k), k..]
+// (k <= 64), with the LUHOT_UPDATE_* engine; asynchronous.
+int fp64_schur_update(luhot_ctx* ctx, double* a, int64_t lda, int k, int m, int n, int engine);
 
 // Solve with device factors: X (n x nrhs, ldx) <- op(A)^-1 B.  b and x may be
 // the same buffer.
@@ -167,11 +172,11 @@ int getrs_apply(luhot_ctx* ctx, int n, int nrhs, const T* lu, int64_t lda, const
 // x = U^-1 L^-1 P b, b and x strided (x may alias b), v1 and v2 n-vector
 // scratch.  Fast mode, untransposed; results agree with getrs_apply to
 // fast-mode rounding.
-// (T = float: tiles of an FP32 factor, formed in FP64 arithmetic and stored
-// in FP32, for the FP64-arithmetic preconditioner of GMRES-IR.)
-template <typename T>
-int scale_factor_blocks(luhot_ctx* ctx, int n, const T* lu, int64_t lda, const double* dinv_l, const double* dinv_u,
-                        T* w, int64_t ldw);
+// (TA = float: FP64 tiles of an FP32 factor, for the FP64-arithmetic
+// preconditioner of GMRES-IR.)
+template <typename TA, typename TW>
+int scale_factor_blocks(luhot_ctx* ctx, int n, const TA* lu, int64_t lda, const double* dinv_l, const double* dinv_u,
+                        TW* w, int64_t ldw);
 // One block-scaled sweep y = T^-1 b (b contiguous, y with stride ldy, y not
 // aliasing b) on the context's stream with fresh tagged-word scratch.
 template <typename TW>

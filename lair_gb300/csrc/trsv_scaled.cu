@@ -111,23 +111,6 @@ __device__ __forceinline__ void scaled_load_row8(double (&d)[8], const double* _
     for (int e = 0; e < 8; ++e) d[e] = (i < n && j + e < n) ? __ldg(src + e) : 0.0;
   }
 }
-__device__ __forceinline__ void scaled_load_row8(double (&d)[8], const float* __restrict__ w, int64_t ldw, int i,
-                                                 int j, int n) {
-  const float* src = w + (int64_t)i * ldw + j;
-  if (i < n && j + 8 <= n) {
-#pragma unroll
-    for (int q = 0; q < 2; ++q) {
-      const float4 v = __ldg(reinterpret_cast<const float4*>(src) + q);
-      d[4 * q] = v.x;
-      d[4 * q + 1] = v.y;
-      d[4 * q + 2] = v.z;
-      d[4 * q + 3] = v.w;
-    }
-  } else {
-#pragma unroll
-    for (int e = 0; e < 8; ++e) d[e] = (i < n && j + e < n) ? static_cast<double>(__ldg(src + e)) : 0.0;
-  }
-}
 
 // Whether a lane's quad of tagged words (values 2L and 2L + 1 of a block of
 // `count` published values) carries this launch's epoch.
@@ -276,11 +259,8 @@ cudaError_t launch_trsv_scaled(cudaStream_t stream, const TW* w, int64_t ldw, co
 
 template cudaError_t launch_scale_blocks<double, double>(cudaStream_t, const double*, int64_t, const double*,
                                                          const double*, double*, int64_t, int);
-template cudaError_t launch_scale_blocks<float, float>(cudaStream_t, const float*, int64_t, const double*,
-                                                       const double*, float*, int64_t, int);
-template cudaError_t launch_trsv_scaled<float>(cudaStream_t, const float*, int64_t, const double*, const double*,
-                                               double*, int64_t, int, bool, unsigned long long*, unsigned int, int*,
-                                               DeviceStatus*);
+template cudaError_t launch_scale_blocks<float, double>(cudaStream_t, const float*, int64_t, const double*,
+                                                        const double*, double*, int64_t, int);
 template cudaError_t launch_trsv_scaled<double>(cudaStream_t, const double*, int64_t, const double*, const double*,
                                                 double*, int64_t, int, bool, unsigned long long*, unsigned int, int*,
                                                 DeviceStatus*);

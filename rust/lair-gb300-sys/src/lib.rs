@@ -25,6 +25,10 @@ pub const LUHOT_ERR_UNSUPPORTED: c_int = 7;
 pub const LUHOT_MODE_FAST: c_int = 0;
 pub const LUHOT_MODE_EXACT: c_int = 1;
 
+pub const LUHOT_UPDATE_AUTO: c_int = 0;
+pub const LUHOT_UPDATE_DMMA: c_int = 1;
+pub const LUHOT_UPDATE_OZAKI: c_int = 2;
+
 pub const LUHOT_PREC_FP32: c_int = 0;
 pub const LUHOT_PREC_BF16: c_int = 1;
 pub const LUHOT_PREC_FP16: c_int = 2;
@@ -80,6 +84,9 @@ extern "C" {
     pub fn luhot_last_error(ctx: *const luhot_ctx) -> *const c_char;
     pub fn luhot_set_stream(ctx: *mut luhot_ctx, cuda_stream: *mut c_void) -> c_int;
     pub fn luhot_set_block(ctx: *mut luhot_ctx, nb: c_int) -> c_int;
+    pub fn luhot_set_fp64_update(ctx: *mut luhot_ctx, engine: c_int) -> c_int;
+    pub fn luhot_dschur_update_dev(ctx: *mut luhot_ctx, m: i64, n: i64, k: i64, d_a: *mut f64, lda: i64,
+                                   engine: c_int) -> c_int;
     pub fn luhot_launch_count(ctx: *const luhot_ctx) -> i64;
     pub fn luhot_selftest_wait_timeout(ctx: *mut luhot_ctx, timeout_ms: i64) -> c_int;
     pub fn luhot_profile_enable(ctx: *mut luhot_ctx, on: c_int) -> c_int;
