@@ -278,16 +278,17 @@ struct IrRun {
   // factors, not on u_low * kappa of each application.
   // FP64 arithmetic is slow on this part, so these sweeps keep 64-row
   // blocks (a quarter of the per-step FP64 work of the chained 128-row form).
-  int lo_solve64(const double* v, double* out) {
-    // After kScaledAfter applications (a long GMRES run), the block-scaled
-    // tiles of the factors are formed once, in FP64 arithmetic and FP64
-    // storage, and every later application uses the block-scaled sweeps,
-    // whose critical path per 64-row block is a quarter of the FMAs.  The
-    // tiles stay in FP64: rounding W = D^-1 T to FP32 perturbs the applied
-    // factor by up to 2^-24 cond(D) relative, and on the weak (TF32, FP16,
-    // BF16) factors, whose GMRES runs take hundreds of iterations, that
-    // perturbation cost up to twice the iterations.
-    if (!w64 && ++minv_calls > kScaledAfter && n > 64) {
+  int lo_solve64(const double* v, double* out, bool cycle_start) {
+    // A long GMRES run (more than kScaledAfter applications) switches to the
+    // block-scaled sweeps, whose critical path per 64-row block is a quarter
+    // of the FMAs: the tiles W = D^-1 T of the factors are formed once, in
+    // FP64 arithmetic and FP64 storage.  The switch happens only where a
+    // restart cycle begins, so every Krylov basis is built with one operator:
+    // the two forms agree only to rounding (relative 2^-53 cond(D)), and a
+    // mid-cycle change breaks the Arnoldi relation that the cycle's residual
+    // estimate rests on.
+    ++minv_calls;
+    if (!w64 && cycle_start && minv_calls > kScaledAfter && n > 64) {
       if (ensure_buf(ctx, ctx->scaled_buf, (size_t)n * ldlo * sizeof(double)) == LUHOT_OK) {
         double* w = static_cast<double*>(ctx->scaled_buf.ptr);
         int rc = scale_factor_blocks(ctx, n, lu, ldlo, dl64, du64, w, ldlo);
@@ -379,7 +380,7 @@ struct IrRun {
   int gmres_cycle(double* x, int* inner) {
     const int m = kGmresRestart;
     // v0 = M^-1 r / ||M^-1 r||_2
-    int rc = lo_solve64(r, t);
+    int rc = lo_solve64(r, t, true);
     if (rc) return rc;
     rc = zero_scalar(kNrm2);
     if (rc) return rc;
@@ -401,7 +402,7 @@ struct IrRun {
       double* vk1 = V + (int64_t)(k + 1) * n;
       rc = matvec(vk, r);  // r is free as scratch inside the cycle
       if (rc) return rc;
-      rc = lo_solve64(r, vk1);
+      rc = lo_solve64(r, vk1, false);
       if (rc) return rc;
       // Two passes of classical Gram-Schmidt against v_0..v_k.
       std::vector<double> hcol(k + 2, 0.0);

@@ -26,25 +26,33 @@
 //   against 4.2e-16 for a plain FP64 GEMM).
 // Combine (epilogue).  R = sum_G T_G 2^(38-8G) in 64-bit fixed point, formed by
 //   Horner from G = 7 down (each step truncates below 2^-38 of T_0's unit;
-//   |R| < 2^62), then C = fma(R, -2^(ea+eb-54), C): one rounding of R to 53
-//   bits and one of the subtraction.  Rows or columns holding Inf or NaN give
+//   |R| < 2^62), then C = C - R 2^(ea+eb-54): one rounding of R to 53 bits
+//   (built with integer operations) and one of the subtraction.  Rows or columns holding Inf or NaN give
 //   NaN in the elements they touch.
 //
-// oz_gemm_kernel: persistent, one CTA per SM, 128 x 64 output tiles in row
-// order, a contiguous range per CTA.  Ten warps:
+// oz_gemm_kernel: persistent, one CTA per SM, 128 x 128 output tiles in row
+// order, a contiguous range per CTA.  An M = 128 MMA costs the tensor pipe
+// about the same time for any N up to 256 (measured: ~128 cycles at N = 64),
+// so the tile is as wide as TMEM allows: two 128-column FP32 accumulators and
+// the 64-bit fixed-point sums of the 128 x 128 tile (256 columns).  Ten warps:
 //   warp 0      TMA producer: the seven 128-row A slices of the CTA's current
-//               row block (112 KB, reloaded when the row block changes) and a
-//               two-stage ring of the seven 64-row B slices of each tile
-//               (56 KB per stage), 3-D tensor maps (k, row, slice), 128-byte
-//               swizzle, rows past M or N zero-filled;
-//   warp 1      TMEM owner (512 columns: one 64-column FP32 accumulator per
-//               group) and MMA issuer: per tile and group G (7 down to 0) the
-//               group's slice products, 4 k-steps of M=128, N=64, K=16 each,
-//               then a commit to that group's full barrier;
+//               row block (112 KB, reloaded when the row block changes) and
+//               the seven 128-row B slices of each tile (112 KB), one barrier
+//               pair per slice: slice q is last read by group G = q, so the
+//               slices free up in the order the next tile needs them (6 .. 0);
+//               3-D tensor maps (k, row, slice), 128-byte swizzle, rows past M
+//               or N zero-filled;
+//   warp 1      TMEM owner (512 columns) and MMA issuer: per tile, groups
+//               G = 7 .. 0, each into accumulator (7 - G) % 2: the group's
+//               slice products, 4 k-steps of M = 128, N = 128, K = 16 each,
+//               then a commit to that accumulator's full barrier;
 //   warps 2-9   epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (tile
-//               rows) and 32 of the 64 columns ((w - 2) / 4); it drains each
-//               group as soon as it is complete and releases it, so the next
-//               tile's MMAs on that group overlap this tile's combine.
+//               rows) and 64 of the 128 columns ((w - 2) / 4): per group it
+//               folds the accumulator into the sums held in TMEM, 16 columns
+//               at a time, and releases the accumulator, so the MMAs of the
+//               next group (and of the next tile) overlap the epilogue; after
+//               group 0 it applies the sums to C (16-byte loads and stores,
+//               one FP64 subtraction per element).
 // All mbarrier waits are bounded by the context's wait limit; on expiry a role
 // records the error and raises the CTA's abort flag, the others stop at their
 // next wait, and before exit the CTA waits (bounded) for its copies and MMAs
@@ -65,17 +73,17 @@ namespace luhot {
 constexpr int kOzSlices = 7;
 constexpr int kOzGroups = 8;   // G = p + q = 0 .. 7
 constexpr int kOzK = 64;       // K of one update (one 128-byte box row of FP16)
-constexpr int kOzBM = 128, kOzBN = 64;
+constexpr int kOzBM = 128, kOzBN = 128;
 constexpr int kOzFrac = 38;    // fractional bits of the fixed-point combine
 constexpr int kOzEpiWarps = 8;
 constexpr int kOzThreads = 64 + 32 * kOzEpiWarps;
-constexpr int kOzABytes = kOzBM * 128;  // one A slice box: 128 rows x 128 B
-constexpr int kOzBBytes = kOzBN * 128;  // one B slice box: 64 rows x 128 B
-constexpr int kOzStages = 2;
-constexpr size_t kOzSmem = 1024 + (size_t)kOzSlices * kOzABytes + (size_t)kOzStages * kOzSlices * kOzBBytes;
+constexpr int kOzSliceBytes = 128 * 128;  // one slice box: 128 rows x 128 B
+constexpr int kOzAccBufs = 2;           // TMEM accumulators of 128 columns, one group each at a time
+constexpr unsigned kOzRCol = 256;       // TMEM columns 256-511: the fixed-point sums (2 words per tile column)
+constexpr size_t kOzSmem = 1024 + 2 * (size_t)kOzSlices * kOzSliceBytes;
 constexpr int kOzNonFinite = 1 << 20;  // exponent of a row / column that holds Inf or NaN
 constexpr int kOzZero = -(1 << 20);    // exponent of a zero element
-static_assert(kOzGroups * kOzBN <= 512, "one TMEM accumulator per group");
+static_assert(kOzAccBufs * kOzBN <= (int)kOzRCol && kOzRCol + 2 * kOzBN <= 512, "accumulators and sums fit in TMEM");
 
 // ---------------------------------------------------------------------------
 // Split.
@@ -231,36 +239,125 @@ __device__ __forceinline__ void oz_tma3d(unsigned dst, const CUtensorMap* map, i
       : "memory");
 }
 
+// TMEM loads and stores of one warp: its 32 lanes, 16, 32 or 64 consecutive
+// 32-bit columns from taddr (lane field in bits 16+).
+__device__ __forceinline__ void tmem_ld16(unsigned taddr, unsigned (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_ld32(unsigned taddr, unsigned (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_st32(unsigned taddr, const unsigned (&r)[32]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,"
+      "%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};"
+      ::"r"(taddr), "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]),
+        "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15]), "r"(r[16]),
+        "r"(r[17]), "r"(r[18]), "r"(r[19]), "r"(r[20]), "r"(r[21]), "r"(r[22]), "r"(r[23]), "r"(r[24]),
+        "r"(r[25]), "r"(r[26]), "r"(r[27]), "r"(r[28]), "r"(r[29]), "r"(r[30]), "r"(r[31])
+      : "memory");
+}
+__device__ __forceinline__ void tmem_ld64(unsigned taddr, unsigned (&r)[64]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x64.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,"
+      "%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,"
+      "%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%64];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]),
+        "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]),
+        "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]),
+        "=r"(r[48]), "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]),
+        "=r"(r[56]), "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_st64(unsigned taddr, const unsigned (&r)[64]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x64.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,"
+      "%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32,"
+      "%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,%48,"
+      "%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63,%64};"
+      ::"r"(taddr), "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]),
+        "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15]), "r"(r[16]),
+        "r"(r[17]), "r"(r[18]), "r"(r[19]), "r"(r[20]), "r"(r[21]), "r"(r[22]), "r"(r[23]), "r"(r[24]),
+        "r"(r[25]), "r"(r[26]), "r"(r[27]), "r"(r[28]), "r"(r[29]), "r"(r[30]), "r"(r[31]), "r"(r[32]),
+        "r"(r[33]), "r"(r[34]), "r"(r[35]), "r"(r[36]), "r"(r[37]), "r"(r[38]), "r"(r[39]), "r"(r[40]),
+        "r"(r[41]), "r"(r[42]), "r"(r[43]), "r"(r[44]), "r"(r[45]), "r"(r[46]), "r"(r[47]), "r"(r[48]),
+        "r"(r[49]), "r"(r[50]), "r"(r[51]), "r"(r[52]), "r"(r[53]), "r"(r[54]), "r"(r[55]), "r"(r[56]),
+        "r"(r[57]), "r"(r[58]), "r"(r[59]), "r"(r[60]), "r"(r[61]), "r"(r[62]), "r"(r[63])
+      : "memory");
+}
+
 __device__ __forceinline__ void oz_commit(unsigned bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
 
-// C - R 2^s for the fixed-point R; NaN when a row or column held Inf / NaN.
+// C - R 2^s for the fixed-point R (s = ea + eb - 54); NaN when a row or
+// column held Inf or NaN.  R 2^s is rounded to 53 bits (to nearest, ties to
+// even, as a conversion of R would) and assembled with integer operations
+// whenever it is a normal number, so the FP64 pipe runs one subtraction per
+// element; zeros, subnormal and overflowing products take the library path.
 __device__ __forceinline__ double oz_combine(long long R, int ea_i, int eb_j, double c) {
   if (ea_i >= kOzNonFinite || eb_j >= kOzNonFinite) return __longlong_as_double(0x7ff8000000000000ll);
   const int s = ea_i + eb_j - (kOzFrac + 16);
-  const double r = __ll2double_rn(R);
-  if (s >= -1022 && s <= 1023) return fma(r, -__longlong_as_double((long long)(s + 1023) << 52), c);
-  return c - scalbn(r, s);
+  const unsigned long long neg = R < 0 ? (1ull << 63) : 0ull;
+  const unsigned long long u = R < 0 ? 0ull - (unsigned long long)R : (unsigned long long)R;
+  const int lz = __clzll((long long)u);            // |R| < 2^62: lz >= 2 (64 when R = 0)
+  const unsigned long long un = u << (lz & 63);    // leading one at bit 63
+  unsigned long long m = un >> 11;                 // 53 bits
+  const unsigned rem = (unsigned)(un & 0x7FF);
+  int t = 63 - lz;                                 // |R| in [2^t, 2^(t+1))
+  m += (rem > 0x400u || (rem == 0x400u && (m & 1))) ? 1ull : 0ull;
+  if (m >> 53) {
+    m >>= 1;
+    ++t;
+  }
+  const int E = t + s + 1023;
+  const unsigned long long frac = m & 0xFFFFFFFFFFFFFull;
+  if (u != 0 && E >= 1 && E <= 2046)
+    return __dsub_rn(c, __longlong_as_double((long long)(neg | ((unsigned long long)E << 52) | frac)));
+  if (u == 0) return __dsub_rn(c, 0.0);
+  if (E > 2046) return __dsub_rn(c, __longlong_as_double((long long)(neg | 0x7FF0000000000000ull)));
+  // Below the normal range: the 53-bit value at exponent -1000 (exact), then
+  // one multiplication by 2^d rounds it once, to the subnormal grid.
+  const int d = E - 23;  // the value is (that number) x 2^d, d < -22
+  if (d < -1074) return __dsub_rn(c, __longlong_as_double((long long)neg));
+  const double mid = __longlong_as_double((long long)(neg | (23ull << 52) | frac));
+  const double p2 = d >= -1022 ? __longlong_as_double((long long)(d + 1023) << 52)
+                               : __longlong_as_double((long long)(1ull << (d + 1074)));
+  return __dsub_rn(c, __dmul_rn(mid, p2));
 }
 
 __global__ void __launch_bounds__(kOzThreads, 1)
-    oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+    oz_gemm_kernel(const __grid_constant__ CUtensorMap tmL, const __grid_constant__ CUtensorMap tmU,
                    double* __restrict__ c, int64_t ldc, int M, int N, const int* __restrict__ ea,
-                   const int* __restrict__ eb, int vec, DeviceStatus* st) {
+                   const int* __restrict__ eb, DeviceStatus* st) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  unsigned char* sA = base;
-  unsigned char* sB = base + (size_t)kOzSlices * kOzABytes;
-  __shared__ __align__(8) unsigned long long a_full, a_empty, b_full[kOzStages], b_empty[kOzStages],
-      g_full[kOzGroups], g_empty[kOzGroups], mma_done;
+  unsigned char* sU = base;                                    // resident: U^T slices of the column block
+  unsigned char* sL = base + (size_t)kOzSlices * kOzSliceBytes;  // streamed: L slices of each tile's rows
+  __shared__ __align__(8) unsigned long long u_full, u_empty, l_full[kOzSlices], l_empty[kOzSlices],
+      acc_full[kOzAccBufs], acc_empty[kOzAccBufs], mma_done;
   __shared__ unsigned tmem_base;
-  __shared__ int s_abort, s_a_issued, s_a_consumed, s_b_issued, s_b_consumed;
+  __shared__ int s_abort, s_u_issued, s_u_consumed, s_l_issued;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const unsigned long long limit = st->timeout_ns;
-  const int tiles_n = (N + kOzBN - 1) / kOzBN;
-  const int tiles = ((M + kOzBM - 1) / kOzBM) * tiles_n;
+  const int tiles_i = (M + kOzBM - 1) / kOzBM;
+  const int tiles = tiles_i * ((N + kOzBN - 1) / kOzBN);
   const int t_begin = (int)((int64_t)blockIdx.x * tiles / gridDim.x);
   const int t_end = (int)((int64_t)(blockIdx.x + 1) * tiles / gridDim.x);
 
@@ -269,19 +366,19 @@ __global__ void __launch_bounds__(kOzThreads, 1)
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   if (threadIdx.x == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&a_full)));
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&a_empty)));
-    for (int s = 0; s < kOzStages; ++s) {
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&b_full[s])));
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&b_empty[s])));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&u_full)));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&u_empty)));
+    for (int p = 0; p < kOzSlices; ++p) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&l_full[p])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&l_empty[p])));
     }
-    for (int g = 0; g < kOzGroups; ++g) {
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&g_full[g])));
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&g_empty[g])), "r"(kOzEpiWarps));
+    for (int b = 0; b < kOzAccBufs; ++b) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&acc_full[b])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&acc_empty[b])), "r"(kOzEpiWarps));
     }
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mma_done)));
     s_abort = 0;
-    s_a_issued = s_a_consumed = s_b_issued = s_b_consumed = 0;
+    s_u_issued = s_u_consumed = s_l_issued = 0;
     asm volatile("fence.mbarrier_init.release.cluster;");
     asm volatile("fence.proxy.async.shared::cta;");
   }
@@ -292,79 +389,88 @@ __global__ void __launch_bounds__(kOzThreads, 1)
 
   if (warp == 0) {
     if (lane == 0) {
-      // Producer.
-      int cur_rb = -1, na = 0, nb = 0;
-      for (int t = t_begin; t < t_end; ++t) {
+      // Producer.  L slices go in the order the MMAs free them (6 .. 0).
+      int cur_jb = -1, nu = 0, tc = 0;
+      for (int t = t_begin; t < t_end; ++t, ++tc) {
         if (*reinterpret_cast<volatile int*>(&s_abort)) break;
-        const int rb = t / tiles_n, cb = t - rb * tiles_n;
-        if (rb != cur_rb) {
-          // The previous row block's slices are free once its last MMAs end.
-          if (na > 0 && !oz_wait(smem_u32(&a_empty), (unsigned)((na - 1) & 1), limit, &s_abort)) {
+        const int jb = t / tiles_i, ib = t - jb * tiles_i;
+        if (jb != cur_jb) {
+          // The previous column block's slices are free once its last MMAs end.
+          if (nu > 0 && !oz_wait(smem_u32(&u_empty), (unsigned)((nu - 1) & 1), limit, &s_abort)) {
             oz_abort(st, &s_abort);
             break;
           }
-          asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(&a_full)),
-                       "r"((unsigned)(kOzSlices * kOzABytes))
+          asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(&u_full)),
+                       "r"((unsigned)(kOzSlices * kOzSliceBytes))
                        : "memory");
-          for (int p = 0; p < kOzSlices; ++p)
-            oz_tma3d(smem_u32(sA + p * kOzABytes), &tmA, rb * kOzBM, p, smem_u32(&a_full));
-          s_a_issued = ++na;
-          cur_rb = rb;
+          for (int q = 0; q < kOzSlices; ++q)
+            oz_tma3d(smem_u32(sU + q * kOzSliceBytes), &tmU, jb * kOzBN, q, smem_u32(&u_full));
+          s_u_issued = ++nu;
+          cur_jb = jb;
         }
-        const int s = nb % kOzStages;
-        if (!oz_wait(smem_u32(&b_empty[s]), (unsigned)((nb / kOzStages) & 1) ^ 1u, limit, &s_abort)) {
+        bool ok = true;
+        for (int p = kOzSlices - 1; p >= 0; --p) {
+          if (!oz_wait(smem_u32(&l_empty[p]), (unsigned)(tc & 1) ^ 1u, limit, &s_abort)) {
+            ok = false;
+            break;
+          }
+          asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(&l_full[p])),
+                       "r"((unsigned)kOzSliceBytes)
+                       : "memory");
+          oz_tma3d(smem_u32(sL + p * kOzSliceBytes), &tmL, ib * kOzBM, p, smem_u32(&l_full[p]));
+          ++s_l_issued;
+        }
+        if (!ok) {
           oz_abort(st, &s_abort);
           break;
         }
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(&b_full[s])),
-                     "r"((unsigned)(kOzSlices * kOzBBytes))
-                     : "memory");
-        unsigned char* sb = sB + (size_t)s * kOzSlices * kOzBBytes;
-        for (int p = 0; p < kOzSlices; ++p)
-          oz_tma3d(smem_u32(sb + p * kOzBBytes), &tmB, cb * kOzBN, p, smem_u32(&b_full[s]));
-        s_b_issued = ++nb;
       }
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      // MMA issuer: D FP32 (bit 4), A and B FP16 (format 0), K-major, N = 64, M = 128.
-      constexpr unsigned idesc = (1u << 4) | ((unsigned)(kOzBN >> 3) << 17) | ((unsigned)(kOzBM >> 4) << 24);
-      int cur_rb = -1, na = 0, nb = 0, tc = 0;
+      // MMA issuer: D FP32 (bit 4), A and B FP16 (format 0), K-major, M = N = 128.
+      // D[j][i] += sum_k U^T_q[j][k] L_p[i][k]: TMEM lanes are columns of C.
+      constexpr unsigned idesc = (1u << 4) | ((unsigned)(kOzBM >> 3) << 17) | ((unsigned)(kOzBN >> 4) << 24);
+      int cur_jb = -1, nu = 0, tc = 0;
       bool ok = true;
       for (int t = t_begin; t < t_end && ok; ++t, ++tc) {
         if (*reinterpret_cast<volatile int*>(&s_abort)) break;
-        const int rb = t / tiles_n;
-        if (rb != cur_rb) {
-          if (!oz_wait(smem_u32(&a_full), (unsigned)(na & 1), limit, &s_abort)) {
+        const int jb = t / tiles_i;
+        if (jb != cur_jb) {
+          if (!oz_wait(smem_u32(&u_full), (unsigned)(nu & 1), limit, &s_abort)) {
             ok = false;
             break;
           }
-          s_a_consumed = ++na;
-          cur_rb = rb;
+          s_u_consumed = ++nu;
+          cur_jb = jb;
         }
-        const int s = nb % kOzStages;
-        if (!oz_wait(smem_u32(&b_full[s]), (unsigned)((nb / kOzStages) & 1), limit, &s_abort)) {
-          ok = false;
-          break;
-        }
-        s_b_consumed = ++nb;
-        asm volatile("tcgen05.fence::after_thread_sync;");
-        const unsigned char* sb = sB + (size_t)s * kOzSlices * kOzBBytes;
-        for (int G = kOzGroups - 1; G >= 0; --G) {
-          // The epilogue has drained this group of the previous tile.
-          if (!oz_wait(smem_u32(&g_empty[G]), (unsigned)(tc & 1) ^ 1u, limit, &s_abort)) {
+        unsigned have = 0;  // L slices of this tile already waited for
+        for (int G = kOzGroups - 1; G >= 0 && ok; --G) {
+          // Group G uses accumulator (7 - G) % 2, as use (7 - G) / 2 of four
+          // per tile: wait for the epilogue's release of the previous use.
+          const int buf = (kOzGroups - 1 - G) & 1;
+          const unsigned use_parity = (unsigned)(((kOzGroups - 1 - G) >> 1) & 1);
+          if (!oz_wait(smem_u32(&acc_empty[buf]), use_parity ^ 1u, limit, &s_abort)) {
             ok = false;
             break;
           }
           asm volatile("tcgen05.fence::after_thread_sync;");
-          const unsigned acc_addr = tmem + (unsigned)(G * kOzBN);
+          const unsigned acc_addr = tmem + (unsigned)(buf * kOzBM);
           unsigned accf = 0;
           for (int p = max(0, G - (kOzSlices - 1)); p <= min(G, kOzSlices - 1); ++p) {
             const int q = G - p;
+            if (!(have & (1u << p))) {
+              if (!oz_wait(smem_u32(&l_full[p]), (unsigned)(tc & 1), limit, &s_abort)) {
+                ok = false;
+                break;
+              }
+              asm volatile("tcgen05.fence::after_thread_sync;");
+              have |= 1u << p;
+            }
 #pragma unroll
             for (int ks = 0; ks < kOzK / 16; ++ks) {
-              const unsigned long long da = sw128_desc(smem_u32(sA + p * kOzABytes + ks * 32));
-              const unsigned long long db = sw128_desc(smem_u32(sb + q * kOzBBytes + ks * 32));
+              const unsigned long long da = sw128_desc(smem_u32(sU + q * kOzSliceBytes + ks * 32));
+              const unsigned long long db = sw128_desc(smem_u32(sL + p * kOzSliceBytes + ks * 32));
               asm volatile(
                   "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, "
                   "p;\n}\n" ::"r"(acc_addr),
@@ -372,12 +478,14 @@ __global__ void __launch_bounds__(kOzThreads, 1)
               accf = 1;
             }
           }
-          oz_commit(smem_u32(&g_full[G]));
+          if (!ok) break;
+          oz_commit(smem_u32(&acc_full[buf]));
+          // L slice G is last used by group G.
+          if (G < kOzSlices) oz_commit(smem_u32(&l_empty[G]));
         }
         if (!ok) break;
-        oz_commit(smem_u32(&b_empty[s]));
-        const bool row_ends = (t + 1 >= t_end) || ((t + 1) / tiles_n != rb);
-        if (row_ends) oz_commit(smem_u32(&a_empty));
+        const bool block_ends = (t + 1 >= t_end) || ((t + 1) / tiles_i != jb);
+        if (block_ends) oz_commit(smem_u32(&u_empty));
       }
       if (!ok) oz_abort(st, &s_abort);
       // Arrives once every MMA issued above has completed.
@@ -385,75 +493,112 @@ __global__ void __launch_bounds__(kOzThreads, 1)
       mbar_wait(smem_u32(&mma_done), 0u, limit);
     }
   } else {
-    // Epilogue.
+    // Epilogue: warp w owns TMEM lanes 32 (w % 4) .. + 31 (32 columns of the
+    // tile) and 64 of its 128 rows, h = (w - 2) / 4.  Its fixed-point sums
+    // stay in TMEM (tile row r: words kOzRCol + 2r, + 2r + 1); 16 rows at a
+    // time pass through registers.
     const int quarter = warp & 3, half = (warp - 2) >> 2;
-    int tc = 0;
-    for (int t = t_begin; t < t_end; ++t, ++tc) {
-      const int rb = t / tiles_n, cb = t - rb * tiles_n;
-      long long R[32];
+    const unsigned lane_base = tmem + ((unsigned)(quarter * 32) << 16);
+    const unsigned r_base = lane_base + kOzRCol + (unsigned)(half * 2 * 64);
+    for (int t = t_begin; t < t_end; ++t) {
+      const int jb = t / tiles_i, ib = t - jb * tiles_i;
+      const int col = jb * kOzBN + quarter * 32 + lane;
+      const int row0 = ib * kOzBM + half * 64;
+      const bool col_ok = col < N;
+      {
+        // Bring this warp's 64 rows x 32 columns of C into L2 while the
+        // tile's products run (lane r: rows r and 32 + r, 256 bytes each).
+        const int c0 = jb * kOzBN + quarter * 32;
+        if (c0 < N) {
+#pragma unroll
+          for (int e = 0; e < 2; ++e) {
+            const int rr = row0 + lane + 32 * e;
+            if (rr < M) {
+              const double* pr = c + (int64_t)rr * ldc + c0;
+              asm volatile("prefetch.global.L2 [%0];" ::"l"(pr));
+              if (c0 + 16 < N) asm volatile("prefetch.global.L2 [%0];" ::"l"(pr + 16));
+            }
+          }
+        }
+      }
       bool ok = true;
       for (int G = kOzGroups - 1; G >= 0; --G) {
-        const bool got = oz_wait(smem_u32(&g_full[G]), (unsigned)(tc & 1), limit, &s_abort);
+        const int buf = (kOzGroups - 1 - G) & 1;
+        const unsigned use_parity = (unsigned)(((kOzGroups - 1 - G) >> 1) & 1);
+        const bool got = oz_wait(smem_u32(&acc_full[buf]), use_parity, limit, &s_abort);
         if (!__all_sync(0xffffffffu, got)) {
           ok = false;
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;");
-        unsigned r[32];
-        const unsigned taddr = tmem + ((unsigned)(quarter * 32) << 16) + (unsigned)(G * kOzBN + half * 32);
-        asm volatile(
-            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,"
-            "%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-              "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-              "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-            : "r"(taddr));
-        asm volatile("tcgen05.wait::ld.sync.aligned;");
+        {
+#pragma unroll 1
+          for (int cc = 0; cc < 2; ++cc) {
+            unsigned tv[32], rv[64];
+            tmem_ld32(lane_base + (unsigned)(buf * kOzBM + half * 64 + cc * 32), tv);
+            if (G < kOzGroups - 1) tmem_ld64(r_base + (unsigned)(cc * 64), rv);
+            asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+            for (int r = 0; r < 32; ++r) {
+              const long long prev =
+                  G < kOzGroups - 1 ? (long long)(((unsigned long long)rv[2 * r + 1] << 32) | rv[2 * r]) : 0ll;
+              const long long Rn = ((long long)__float2int_rn(__uint_as_float(tv[r])) << kOzFrac) + (prev >> 8);
+              rv[2 * r] = (unsigned)(unsigned long long)Rn;
+              rv[2 * r + 1] = (unsigned)((unsigned long long)Rn >> 32);
+            }
+            tmem_st64(r_base + (unsigned)(cc * 64), rv);
+          }
+          asm volatile("tcgen05.wait::st.sync.aligned;");
+        }
+        // This warp has read the accumulator: the MMA warp may reuse it.
         asm volatile("tcgen05.fence::before_thread_sync;");
         __syncwarp();
-        if (lane == 0) mbar_arrive(smem_u32(&g_empty[G]));
-        if (G == kOzGroups - 1) {
-#pragma unroll
-          for (int j = 0; j < 32; ++j) R[j] = (long long)__float2int_rn(__uint_as_float(r[j])) << kOzFrac;
-        } else {
-#pragma unroll
-          for (int j = 0; j < 32; ++j)
-            R[j] = ((long long)__float2int_rn(__uint_as_float(r[j])) << kOzFrac) + (R[j] >> 8);
-        }
+        if (lane == 0) mbar_arrive(smem_u32(&acc_empty[buf]));
       }
       if (!ok) {
         if (lane == 0) oz_abort(st, &s_abort);
         break;
       }
-      const int row = rb * kOzBM + quarter * 32 + lane;
-      const int col0 = cb * kOzBN + half * 32;
-      if (row < M) {
-        const int ea_i = ea[row];
-        double* crow = c + (int64_t)row * ldc + col0;
-        if (vec && col0 + 32 <= N) {
+      // C -= the sums: thread = one column of C, 64 of the tile's rows in
+      // chunks of 8; a warp's loads and stores of one row are 32 consecutive
+      // doubles.  Lane r holds the exponents of rows r and 32 + r.
+      const int eb_j = col_ok ? eb[col] : 0;
+      const int my_ea0 = row0 + lane < M ? ea[row0 + lane] : 0;
+      const int my_ea1 = row0 + 32 + lane < M ? ea[row0 + 32 + lane] : 0;
+      double* ccol = c + (int64_t)row0 * ldc + (col_ok ? col : 0);
+#pragma unroll 1
+      for (int cc = 0; cc < 8; ++cc) {
+        unsigned rv[16];
+        tmem_ld16(r_base + (unsigned)(cc * 16), rv);
+        const double* src = ccol + (int64_t)(8 * cc) * ldc;
+        double cv[8];
 #pragma unroll
-          for (int q = 0; q < 16; ++q) {
-            const int2 e2 = *reinterpret_cast<const int2*>(eb + col0 + 2 * q);
-            double2 v = *reinterpret_cast<const double2*>(crow + 2 * q);
-            v.x = oz_combine(R[2 * q], ea_i, e2.x, v.x);
-            v.y = oz_combine(R[2 * q + 1], ea_i, e2.y, v.y);
-            *reinterpret_cast<double2*>(crow + 2 * q) = v;
-          }
-        } else {
+        for (int r = 0; r < 8; ++r) cv[r] = (col_ok && row0 + 8 * cc + r < M) ? __ldcs(src + r * ldc) : 0.0;
+        asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
-          for (int j = 0; j < 32; ++j)
-            if (col0 + j < N) crow[j] = oz_combine(R[j], ea_i, eb[col0 + j], crow[j]);
+        for (int r = 0; r < 8; ++r) {
+          const int rr = 8 * cc + r;
+          const long long R = (long long)(((unsigned long long)rv[2 * r + 1] << 32) | rv[2 * r]);
+          const int ea_i = __shfl_sync(0xffffffffu, rr < 32 ? my_ea0 : my_ea1, rr & 31);
+          cv[r] = oz_combine(R, ea_i, eb_j, cv[r]);
         }
+        double* dst = ccol + (int64_t)(8 * cc) * ldc;
+#pragma unroll
+        for (int r = 0; r < 8; ++r)
+          if (col_ok && row0 + 8 * cc + r < M) __stcs(dst + r * ldc, cv[r]);
       }
     }
   }
   __syncthreads();
   if (threadIdx.x == 0 && s_abort) {
     // Copies issued but never consumed must land before the CTA exits.
-    if (s_a_issued > s_a_consumed) mbar_wait(smem_u32(&a_full), (unsigned)((s_a_issued - 1) & 1), limit);
-    for (int i = s_b_consumed; i < s_b_issued; ++i)
-      mbar_wait(smem_u32(&b_full[i % kOzStages]), (unsigned)((i / kOzStages) & 1), limit);
+    if (s_u_issued > s_u_consumed) mbar_wait(smem_u32(&u_full), (unsigned)((s_u_issued - 1) & 1), limit);
+    // L slices: every issued slice's barrier completes once its bytes land
+    // (issue order 6 .. 0 per tile).
+    for (int p = 0; p < kOzSlices; ++p) {
+      const int uses = s_l_issued / kOzSlices + (kOzSlices - 1 - p < s_l_issued % kOzSlices ? 1 : 0);
+      if (uses > 0) mbar_wait(smem_u32(&l_full[p]), (unsigned)((uses - 1) & 1), limit);
+    }
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
@@ -516,16 +661,15 @@ int ozaki_update(luhot_ctx* ctx, double* a, int64_t lda, int k0, int w, int r1, 
   prof_end(ctx, kProfOther, 0.0, (double)N * w * 8 + (double)N * kOzK * kOzSlices * 2);
   LUHOT_CUDA_TRY(ctx, cudaGetLastError());
 
-  CUtensorMap tmA, tmB;
-  int rc = make_slice_map(ctx, &tmA, as, M, kOzBM);
-  if (!rc) rc = make_slice_map(ctx, &tmB, bs, N, kOzBN);
+  CUtensorMap tmL, tmU;
+  int rc = make_slice_map(ctx, &tmL, as, M, kOzBM);
+  if (!rc) rc = make_slice_map(ctx, &tmU, bs, N, kOzBN);
   if (rc) return rc;
   double* cb = a + (int64_t)r1 * lda + c1;
-  const int vec = (lda % 2 == 0) && (reinterpret_cast<uintptr_t>(cb) % 16 == 0) ? 1 : 0;
   const int tiles = ((M + kOzBM - 1) / kOzBM) * ((N + kOzBN - 1) / kOzBN);
   LUHOT_CUDA_TRY(ctx, allow_max_dynamic_smem(oz_gemm_kernel));
   prof_begin(ctx, kProfGemm);
-  oz_gemm_kernel<<<std::min(tiles, ctx->num_sms), kOzThreads, kOzSmem, stream>>>(tmA, tmB, cb, lda, M, N, ea, eb, vec,
+  oz_gemm_kernel<<<std::min(tiles, ctx->num_sms), kOzThreads, kOzSmem, stream>>>(tmL, tmU, cb, lda, M, N, ea, eb,
                                                                                 ctx->d_status);
   // algorithmic work: 2MNK FP64 flops; bytes: C read + written, the slices read once
   prof_end(ctx, kProfGemm, 2.0 * M * N * w,
