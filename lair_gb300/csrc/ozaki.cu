@@ -75,7 +75,7 @@ constexpr int kOzGroups = 8;   // G = p + q = 0 .. 7
 constexpr int kOzK = 64;       // K of one update (one 128-byte box row of FP16)
 constexpr int kOzBM = 128, kOzBN = 128;
 constexpr int kOzFrac = 38;    // fractional bits of the fixed-point combine
-constexpr int kOzEpiWarps = 8;
+constexpr int kOzEpiWarps = 16;
 constexpr int kOzThreads = 64 + 32 * kOzEpiWarps;
 constexpr int kOzSliceBytes = 128 * 128;  // one slice box: 128 rows x 128 B
 constexpr int kOzAccBufs = 2;           // TMEM accumulators of 128 columns, one group each at a time
@@ -305,21 +305,21 @@ __device__ __forceinline__ void oz_commit(unsigned bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
 
-// C - R 2^s for the fixed-point R (s = ea + eb - 54); NaN when a row or
-// column held Inf or NaN.  R 2^s is rounded to 53 bits (to nearest, ties to
-// even, as a conversion of R would) and assembled with integer operations
-// whenever it is a normal number, so the FP64 pipe runs one subtraction per
-// element; zeros, subnormal and overflowing products take the library path.
-__device__ __forceinline__ double oz_combine(long long R, int ea_i, int eb_j, double c) {
-  if (ea_i >= kOzNonFinite || eb_j >= kOzNonFinite) return __longlong_as_double(0x7ff8000000000000ll);
-  const int s = ea_i + eb_j - (kOzFrac + 16);
+// C - R 2^s for the fixed-point R = hi 2^32 + lo (s = ea + eb - 54); NaN
+// when a row or column held Inf or NaN.  R 2^s is rounded to 53 bits (to
+// nearest, ties to even, as a conversion of R would) and assembled with
+// 32-bit integer operations whenever it is a normal number, so the FP64 pipe
+// runs one subtraction per element; zeros, subnormal and overflowing
+// products take the general path.
+__device__ __noinline__ double oz_combine_rare(long long R, int s, double c) {
   const unsigned long long neg = R < 0 ? (1ull << 63) : 0ull;
   const unsigned long long u = R < 0 ? 0ull - (unsigned long long)R : (unsigned long long)R;
-  const int lz = __clzll((long long)u);            // |R| < 2^62: lz >= 2 (64 when R = 0)
-  const unsigned long long un = u << (lz & 63);    // leading one at bit 63
-  unsigned long long m = un >> 11;                 // 53 bits
+  if (u == 0) return __dsub_rn(c, 0.0);
+  const int lz = __clzll((long long)u);
+  const unsigned long long un = u << lz;
+  unsigned long long m = un >> 11;
   const unsigned rem = (unsigned)(un & 0x7FF);
-  int t = 63 - lz;                                 // |R| in [2^t, 2^(t+1))
+  int t = 63 - lz;
   m += (rem > 0x400u || (rem == 0x400u && (m & 1))) ? 1ull : 0ull;
   if (m >> 53) {
     m >>= 1;
@@ -327,9 +327,8 @@ __device__ __forceinline__ double oz_combine(long long R, int ea_i, int eb_j, do
   }
   const int E = t + s + 1023;
   const unsigned long long frac = m & 0xFFFFFFFFFFFFFull;
-  if (u != 0 && E >= 1 && E <= 2046)
+  if (E >= 1 && E <= 2046)
     return __dsub_rn(c, __longlong_as_double((long long)(neg | ((unsigned long long)E << 52) | frac)));
-  if (u == 0) return __dsub_rn(c, 0.0);
   if (E > 2046) return __dsub_rn(c, __longlong_as_double((long long)(neg | 0x7FF0000000000000ull)));
   // Below the normal range: the 53-bit value at exponent -1000 (exact), then
   // one multiplication by 2^d rounds it once, to the subnormal grid.
@@ -339,6 +338,31 @@ __device__ __forceinline__ double oz_combine(long long R, int ea_i, int eb_j, do
   const double p2 = d >= -1022 ? __longlong_as_double((long long)(d + 1023) << 52)
                                : __longlong_as_double((long long)(1ull << (d + 1074)));
   return __dsub_rn(c, __dmul_rn(mid, p2));
+}
+
+__device__ __forceinline__ double oz_combine(unsigned hi, unsigned lo, int ea_i, int eb_j, double c) {
+  if (ea_i >= kOzNonFinite || eb_j >= kOzNonFinite) return __longlong_as_double(0x7ff8000000000000ll);
+  const int s = ea_i + eb_j - (kOzFrac + 16);
+  // Common case: |R| >= 2^32 (hi carries the leading one), result normal.
+  const bool neg = (int)hi < 0;
+  const unsigned ul = neg ? 0u - lo : lo;
+  const unsigned uh = neg ? ~hi + (lo == 0u ? 1u : 0u) : hi;  // |R| = uh 2^32 + ul, uh < 2^30
+  const int lz = __clz((int)uh);                              // 2 .. 32
+  if (uh != 0u) {
+    const unsigned nh = __funnelshift_l(ul, uh, lz);  // leading one at bit 31
+    const unsigned nl = ul << lz;
+    unsigned mh = nh >> 11, ml = __funnelshift_r(nl, nh, 11);  // 53 bits: mh has 21
+    const unsigned rem = nl & 0x7FFu;
+    const unsigned inc = (rem > 0x400u || (rem == 0x400u && (ml & 1u))) ? 1u : 0u;
+    ml += inc;
+    mh += (inc & (ml == 0u ? 1u : 0u));
+    const int E = 63 - lz + (int)(mh >> 21) + s + 1023;
+    if (E >= 1 && E <= 2046) {
+      const unsigned dh = (neg ? 0x80000000u : 0u) | ((unsigned)E << 20) | (mh & 0xFFFFFu);
+      return __dsub_rn(c, __hiloint2double((int)dh, (int)ml));
+    }
+  }
+  return oz_combine_rare((long long)(((unsigned long long)hi << 32) | lo), s, c);
 }
 
 __global__ void __launch_bounds__(kOzThreads, 1)
@@ -494,31 +518,25 @@ __global__ void __launch_bounds__(kOzThreads, 1)
     }
   } else {
     // Epilogue: warp w owns TMEM lanes 32 (w % 4) .. + 31 (32 columns of the
-    // tile) and 64 of its 128 rows, h = (w - 2) / 4.  Its fixed-point sums
-    // stay in TMEM (tile row r: words kOzRCol + 2r, + 2r + 1); 16 rows at a
-    // time pass through registers.
-    const int quarter = warp & 3, half = (warp - 2) >> 2;
+    // tile) and 32 of its 128 rows, g = (w - 2) / 4.  Its fixed-point sums
+    // stay in TMEM (tile row r: words kOzRCol + 2r (low), + 2r + 1 (high));
+    // 16 rows at a time pass through registers.
+    const int quarter = warp & 3, rq = (warp - 2) >> 2;
     const unsigned lane_base = tmem + ((unsigned)(quarter * 32) << 16);
-    const unsigned r_base = lane_base + kOzRCol + (unsigned)(half * 2 * 64);
+    const unsigned r_base = lane_base + kOzRCol + (unsigned)(rq * 2 * 32);
     for (int t = t_begin; t < t_end; ++t) {
       const int jb = t / tiles_i, ib = t - jb * tiles_i;
       const int col = jb * kOzBN + quarter * 32 + lane;
-      const int row0 = ib * kOzBM + half * 64;
+      const int row0 = ib * kOzBM + rq * 32;
       const bool col_ok = col < N;
       {
-        // Bring this warp's 64 rows x 32 columns of C into L2 while the
-        // tile's products run (lane r: rows r and 32 + r, 256 bytes each).
+        // Bring this warp's 32 rows x 32 columns of C into L2 while the
+        // tile's products run (lane r: row r, 256 bytes).
         const int c0 = jb * kOzBN + quarter * 32;
-        if (c0 < N) {
-#pragma unroll
-          for (int e = 0; e < 2; ++e) {
-            const int rr = row0 + lane + 32 * e;
-            if (rr < M) {
-              const double* pr = c + (int64_t)rr * ldc + c0;
-              asm volatile("prefetch.global.L2 [%0];" ::"l"(pr));
-              if (c0 + 16 < N) asm volatile("prefetch.global.L2 [%0];" ::"l"(pr + 16));
-            }
-          }
+        if (c0 < N && row0 + lane < M) {
+          const double* pr = c + (int64_t)(row0 + lane) * ldc + c0;
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(pr));
+          if (c0 + 16 < N) asm volatile("prefetch.global.L2 [%0];" ::"l"(pr + 16));
         }
       }
       bool ok = true;
@@ -531,26 +549,30 @@ __global__ void __launch_bounds__(kOzThreads, 1)
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;");
-        {
 #pragma unroll 1
-          for (int cc = 0; cc < 2; ++cc) {
-            unsigned tv[32], rv[64];
-            tmem_ld32(lane_base + (unsigned)(buf * kOzBM + half * 64 + cc * 32), tv);
-            if (G < kOzGroups - 1) tmem_ld64(r_base + (unsigned)(cc * 64), rv);
-            asm volatile("tcgen05.wait::ld.sync.aligned;");
+        for (int cc = 0; cc < 2; ++cc) {
+          unsigned tv[16], rv[32];
+          tmem_ld16(lane_base + (unsigned)(buf * kOzBM + rq * 32 + cc * 16), tv);
+          if (G < kOzGroups - 1) tmem_ld32(r_base + (unsigned)(cc * 32), rv);
+          asm volatile("tcgen05.wait::ld.sync.aligned;");
+          // R = T 2^38 + floor(R / 2^8) on (hi, lo) words: T 2^38 only
+          // touches hi (|R| < 2^62), so no carry crosses the words.
 #pragma unroll
-            for (int r = 0; r < 32; ++r) {
-              const long long prev =
-                  G < kOzGroups - 1 ? (long long)(((unsigned long long)rv[2 * r + 1] << 32) | rv[2 * r]) : 0ll;
-              const long long Rn = ((long long)__float2int_rn(__uint_as_float(tv[r])) << kOzFrac) + (prev >> 8);
-              rv[2 * r] = (unsigned)(unsigned long long)Rn;
-              rv[2 * r + 1] = (unsigned)((unsigned long long)Rn >> 32);
+          for (int r = 0; r < 16; ++r) {
+            const int tg = __float2int_rn(__uint_as_float(tv[r]));
+            if (G < kOzGroups - 1) {
+              const unsigned lo = rv[2 * r], hi = rv[2 * r + 1];
+              rv[2 * r] = __funnelshift_r(lo, hi, 8);
+              rv[2 * r + 1] = (unsigned)(((int)hi >> 8) + (tg << (kOzFrac - 32)));
+            } else {
+              rv[2 * r] = 0u;
+              rv[2 * r + 1] = (unsigned)(tg << (kOzFrac - 32));
             }
-            tmem_st64(r_base + (unsigned)(cc * 64), rv);
           }
-          asm volatile("tcgen05.wait::st.sync.aligned;");
+          tmem_st32(r_base + (unsigned)(cc * 32), rv);
         }
         // This warp has read the accumulator: the MMA warp may reuse it.
+        asm volatile("tcgen05.wait::st.sync.aligned;");
         asm volatile("tcgen05.fence::before_thread_sync;");
         __syncwarp();
         if (lane == 0) mbar_arrive(smem_u32(&acc_empty[buf]));
@@ -559,15 +581,14 @@ __global__ void __launch_bounds__(kOzThreads, 1)
         if (lane == 0) oz_abort(st, &s_abort);
         break;
       }
-      // C -= the sums: thread = one column of C, 64 of the tile's rows in
+      // C -= the sums: thread = one column of C, 32 of the tile's rows in
       // chunks of 8; a warp's loads and stores of one row are 32 consecutive
-      // doubles.  Lane r holds the exponents of rows r and 32 + r.
+      // doubles.  Lane r holds the exponent of row r.
       const int eb_j = col_ok ? eb[col] : 0;
-      const int my_ea0 = row0 + lane < M ? ea[row0 + lane] : 0;
-      const int my_ea1 = row0 + 32 + lane < M ? ea[row0 + 32 + lane] : 0;
+      const int my_ea = row0 + lane < M ? ea[row0 + lane] : 0;
       double* ccol = c + (int64_t)row0 * ldc + (col_ok ? col : 0);
 #pragma unroll 1
-      for (int cc = 0; cc < 8; ++cc) {
+      for (int cc = 0; cc < 4; ++cc) {
         unsigned rv[16];
         tmem_ld16(r_base + (unsigned)(cc * 16), rv);
         const double* src = ccol + (int64_t)(8 * cc) * ldc;
@@ -577,10 +598,8 @@ __global__ void __launch_bounds__(kOzThreads, 1)
         asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
         for (int r = 0; r < 8; ++r) {
-          const int rr = 8 * cc + r;
-          const long long R = (long long)(((unsigned long long)rv[2 * r + 1] << 32) | rv[2 * r]);
-          const int ea_i = __shfl_sync(0xffffffffu, rr < 32 ? my_ea0 : my_ea1, rr & 31);
-          cv[r] = oz_combine(R, ea_i, eb_j, cv[r]);
+          const int ea_i = __shfl_sync(0xffffffffu, my_ea, 8 * cc + r);
+          cv[r] = oz_combine(rv[2 * r + 1], rv[2 * r], ea_i, eb_j, cv[r]);
         }
         double* dst = ccol + (int64_t)(8 * cc) * ldc;
 #pragma unroll
