@@ -74,7 +74,7 @@ int luhot_set_block(luhot_ctx* ctx, int nb);
 /* Schur-update engine of fast-mode FP64 getrf (no lair counterpart).
  * LUHOT_UPDATE_AUTO (default): trailing blocks of at least 256 x 256 are
  * updated on the FP16 tensor cores by an exact integer-slice product (Ozaki
- * scheme: seven 8-bit slices per operand, 34 slice products, FP32 sums that
+ * scheme: seven 8-bit slices per operand, 28 slice products, FP32 sums that
  * are exact, one FP64 rounding; error at or below an FP64 GEMM's), smaller
  * ones on the FP64 tensor cores (DMMA).  LUHOT_UPDATE_DMMA: DMMA only.
  * LUHOT_UPDATE_OZAKI: the tensor-core product on every block of at least

@@ -17,15 +17,15 @@
 //   transposed, Bs[p][j][k] (one 128-byte row per i or j: one TMA box row).
 // Products (oz_gemm_kernel).  With A_p, B_q the digit matrices,
 //       L U = 2^(ea+eb) sum_G T_G 2^(-8(G+2)),   T_G = sum_{p+q=G} A_p B_q^T,
-//   kept for G = 0..7 (34 slice products of the 49).  Every partial sum of
+//   kept for G = 0..6 (28 slice products of the 49).  Every partial sum of
 //   T_G is an integer of magnitude below 9 * 2^20 for K <= 64, so the FP32
-//   accumulation in TMEM is exact.  Dropped groups (G >= 8) weigh less than
-//   2^-57 of 2^(ea+eb), the element roundings 2^-57 of each operand's scale:
-//   the product error is of order K 2^(ea+eb-56), inside FP64's own bound for
-//   a K-term dot product (measured on N(0,1) factors: 2.3e-16 of |L||U|
-//   against 4.2e-16 for a plain FP64 GEMM).
+//   accumulation in TMEM is exact.  The dropped groups (G >= 7) weigh at most
+//   2^-49.4 of 2^(ea+eb) (typically 2^-55), the element roundings 2^-57 of
+//   each operand's scale: the product error stays well inside FP64's own
+//   bound for a K-term dot product (measured on N(0,1) factors: 1.1e-16 of
+//   |C| + |L||U| against 4.7e-16 for the FP64 tensor cores).
 // Combine (epilogue).  R = sum_G T_G 2^(38-8G) in 64-bit fixed point, formed by
-//   Horner from G = 7 down (each step truncates below 2^-38 of T_0's unit;
+//   Horner from G = 6 down (each step truncates below 2^-38 of T_0's unit;
 //   |R| < 2^62), then C = C - R 2^(ea+eb-54): one rounding of R to 53 bits
 //   (built with integer operations) and one of the subtraction.  Rows or columns holding Inf or NaN give
 //   NaN in the elements they touch.
@@ -43,7 +43,7 @@
 //               3-D tensor maps (k, row, slice), 128-byte swizzle, rows past M
 //               or N zero-filled;
 //   warp 1      TMEM owner (512 columns) and MMA issuer: per tile, groups
-//               G = 7 .. 0, each into accumulator (7 - G) % 2: the group's
+//               G = 6 .. 0, taking the three accumulators in turn: the group's
 //               slice products, 4 k-steps of M = 128, N = 128, K = 16 each,
 //               then a commit to that accumulator's full barrier;
 //   warps 2-9   epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (tile
@@ -71,19 +71,19 @@
 namespace luhot {
 
 constexpr int kOzSlices = 7;
-constexpr int kOzGroups = 8;   // G = p + q = 0 .. 7
+constexpr int kOzGroups = 7;   // G = p + q = 0 .. 6
 constexpr int kOzK = 64;       // K of one update (one 128-byte box row of FP16)
 constexpr int kOzBM = 128, kOzBN = 128;
 constexpr int kOzFrac = 38;    // fractional bits of the fixed-point combine
 constexpr int kOzEpiWarps = 16;
 constexpr int kOzThreads = 64 + 32 * kOzEpiWarps;
 constexpr int kOzSliceBytes = 128 * 128;  // one slice box: 128 rows x 128 B
-constexpr int kOzAccBufs = 2;           // TMEM accumulators of 128 columns, one group each at a time
-constexpr unsigned kOzRCol = 256;       // TMEM columns 256-511: the fixed-point sums (2 words per tile column)
+constexpr int kOzAccBufs = 3;           // TMEM accumulators of 128 columns, used in turn by the groups
+constexpr unsigned kOzLoCol = 384;      // TMEM columns 384-511: low words of the fixed-point sums
 constexpr size_t kOzSmem = 1024 + 2 * (size_t)kOzSlices * kOzSliceBytes;
 constexpr int kOzNonFinite = 1 << 20;  // exponent of a row / column that holds Inf or NaN
 constexpr int kOzZero = -(1 << 20);    // exponent of a zero element
-static_assert(kOzAccBufs * kOzBN <= (int)kOzRCol && kOzRCol + 2 * kOzBN <= 512, "accumulators and sums fit in TMEM");
+static_assert(kOzAccBufs * kOzBM <= (int)kOzLoCol && kOzLoCol + kOzBM <= 512, "accumulators and sums fit in TMEM");
 
 // ---------------------------------------------------------------------------
 // Split.
@@ -239,7 +239,7 @@ __device__ __forceinline__ void oz_tma3d(unsigned dst, const CUtensorMap* map, i
       : "memory");
 }
 
-// TMEM loads and stores of one warp: its 32 lanes, 16, 32 or 64 consecutive
+// TMEM loads and stores of one warp: its 32 lanes, 4, 8, 16 or 32 consecutive
 // 32-bit columns from taddr (lane field in bits 16+).
 __device__ __forceinline__ void tmem_ld16(unsigned taddr, unsigned (&r)[16]) {
   asm volatile(
@@ -268,36 +268,22 @@ __device__ __forceinline__ void tmem_st32(unsigned taddr, const unsigned (&r)[32
         "r"(r[25]), "r"(r[26]), "r"(r[27]), "r"(r[28]), "r"(r[29]), "r"(r[30]), "r"(r[31])
       : "memory");
 }
-__device__ __forceinline__ void tmem_ld64(unsigned taddr, unsigned (&r)[64]) {
+__device__ __forceinline__ void tmem_ld4(unsigned taddr, unsigned (&r)[4]) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_ld8(unsigned taddr, unsigned (&r)[8]) {
   asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x64.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,"
-      "%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,"
-      "%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%64];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]),
-        "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]),
-        "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]),
-        "=r"(r[48]), "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]),
-        "=r"(r[56]), "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
       : "r"(taddr));
 }
-__device__ __forceinline__ void tmem_st64(unsigned taddr, const unsigned (&r)[64]) {
+__device__ __forceinline__ void tmem_st16(unsigned taddr, const unsigned (&r)[16]) {
   asm volatile(
-      "tcgen05.st.sync.aligned.32x32b.x64.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,"
-      "%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32,"
-      "%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,%48,"
-      "%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63,%64};"
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};"
       ::"r"(taddr), "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]),
-        "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15]), "r"(r[16]),
-        "r"(r[17]), "r"(r[18]), "r"(r[19]), "r"(r[20]), "r"(r[21]), "r"(r[22]), "r"(r[23]), "r"(r[24]),
-        "r"(r[25]), "r"(r[26]), "r"(r[27]), "r"(r[28]), "r"(r[29]), "r"(r[30]), "r"(r[31]), "r"(r[32]),
-        "r"(r[33]), "r"(r[34]), "r"(r[35]), "r"(r[36]), "r"(r[37]), "r"(r[38]), "r"(r[39]), "r"(r[40]),
-        "r"(r[41]), "r"(r[42]), "r"(r[43]), "r"(r[44]), "r"(r[45]), "r"(r[46]), "r"(r[47]), "r"(r[48]),
-        "r"(r[49]), "r"(r[50]), "r"(r[51]), "r"(r[52]), "r"(r[53]), "r"(r[54]), "r"(r[55]), "r"(r[56]),
-        "r"(r[57]), "r"(r[58]), "r"(r[59]), "r"(r[60]), "r"(r[61]), "r"(r[62]), "r"(r[63])
+        "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])
       : "memory");
 }
 
@@ -311,7 +297,7 @@ __device__ __forceinline__ void oz_commit(unsigned bar) {
 // 32-bit integer operations whenever it is a normal number, so the FP64 pipe
 // runs one subtraction per element; zeros, subnormal and overflowing
 // products take the general path.
-__device__ __noinline__ double oz_combine_rare(long long R, int s, double c) {
+__device__ __forceinline__ double oz_combine_rare(long long R, int s, double c) {
   const unsigned long long neg = R < 0 ? (1ull << 63) : 0ull;
   const unsigned long long u = R < 0 ? 0ull - (unsigned long long)R : (unsigned long long)R;
   if (u == 0) return __dsub_rn(c, 0.0);
@@ -470,10 +456,12 @@ __global__ void __launch_bounds__(kOzThreads, 1)
         }
         unsigned have = 0;  // L slices of this tile already waited for
         for (int G = kOzGroups - 1; G >= 0 && ok; --G) {
-          // Group G uses accumulator (7 - G) % 2, as use (7 - G) / 2 of four
-          // per tile: wait for the epilogue's release of the previous use.
-          const int buf = (kOzGroups - 1 - G) & 1;
-          const unsigned use_parity = (unsigned)(((kOzGroups - 1 - G) >> 1) & 1);
+          // The groups take the accumulators in turn over the whole launch:
+          // group number i = 8 tc + 7 - G uses accumulator i % 3 for its use
+          // i / 3; wait for the epilogue's release of the previous use.
+          const int gi = kOzGroups * tc + kOzGroups - 1 - G;
+          const int buf = gi % kOzAccBufs;
+          const unsigned use_parity = (unsigned)((gi / kOzAccBufs) & 1);
           if (!oz_wait(smem_u32(&acc_empty[buf]), use_parity ^ 1u, limit, &s_abort)) {
             ok = false;
             break;
@@ -518,13 +506,15 @@ __global__ void __launch_bounds__(kOzThreads, 1)
     }
   } else {
     // Epilogue: warp w owns TMEM lanes 32 (w % 4) .. + 31 (32 columns of the
-    // tile) and 32 of its 128 rows, g = (w - 2) / 4.  Its fixed-point sums
-    // stay in TMEM (tile row r: words kOzRCol + 2r (low), + 2r + 1 (high));
-    // 16 rows at a time pass through registers.
+    // tile) and 32 of its 128 rows, g = (w - 2) / 4.  Its thread keeps the
+    // high words of its column's 32 fixed-point sums in registers and the low
+    // words in TMEM (tile row r: column kOzLoCol + r); 16 rows of an
+    // accumulator at a time pass through registers.
     const int quarter = warp & 3, rq = (warp - 2) >> 2;
     const unsigned lane_base = tmem + ((unsigned)(quarter * 32) << 16);
-    const unsigned r_base = lane_base + kOzRCol + (unsigned)(rq * 2 * 32);
-    for (int t = t_begin; t < t_end; ++t) {
+    const unsigned lo_base = lane_base + kOzLoCol + (unsigned)(rq * 32);
+    int tc = 0;
+    for (int t = t_begin; t < t_end; ++t, ++tc) {
       const int jb = t / tiles_i, ib = t - jb * tiles_i;
       const int col = jb * kOzBN + quarter * 32 + lane;
       const int row0 = ib * kOzBM + rq * 32;
@@ -539,37 +529,40 @@ __global__ void __launch_bounds__(kOzThreads, 1)
           if (c0 + 16 < N) asm volatile("prefetch.global.L2 [%0];" ::"l"(pr + 16));
         }
       }
+      unsigned rh[32];
       bool ok = true;
       for (int G = kOzGroups - 1; G >= 0; --G) {
-        const int buf = (kOzGroups - 1 - G) & 1;
-        const unsigned use_parity = (unsigned)(((kOzGroups - 1 - G) >> 1) & 1);
+        const int gi = kOzGroups * tc + kOzGroups - 1 - G;
+        const int buf = gi % kOzAccBufs;
+        const unsigned use_parity = (unsigned)((gi / kOzAccBufs) & 1);
         const bool got = oz_wait(smem_u32(&acc_full[buf]), use_parity, limit, &s_abort);
         if (!__all_sync(0xffffffffu, got)) {
           ok = false;
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;");
-#pragma unroll 1
+#pragma unroll
         for (int cc = 0; cc < 2; ++cc) {
-          unsigned tv[16], rv[32];
+          unsigned tv[16], lv[16];
           tmem_ld16(lane_base + (unsigned)(buf * kOzBM + rq * 32 + cc * 16), tv);
-          if (G < kOzGroups - 1) tmem_ld32(r_base + (unsigned)(cc * 32), rv);
+          if (G < kOzGroups - 1) tmem_ld16(lo_base + (unsigned)(cc * 16), lv);
           asm volatile("tcgen05.wait::ld.sync.aligned;");
           // R = T 2^38 + floor(R / 2^8) on (hi, lo) words: T 2^38 only
           // touches hi (|R| < 2^62), so no carry crosses the words.
 #pragma unroll
           for (int r = 0; r < 16; ++r) {
+            const int k = cc * 16 + r;
             const int tg = __float2int_rn(__uint_as_float(tv[r]));
             if (G < kOzGroups - 1) {
-              const unsigned lo = rv[2 * r], hi = rv[2 * r + 1];
-              rv[2 * r] = __funnelshift_r(lo, hi, 8);
-              rv[2 * r + 1] = (unsigned)(((int)hi >> 8) + (tg << (kOzFrac - 32)));
+              const unsigned hi = rh[k];
+              lv[r] = __funnelshift_r(lv[r], hi, 8);
+              rh[k] = (unsigned)(((int)hi >> 8) + (tg << (kOzFrac - 32)));
             } else {
-              rv[2 * r] = 0u;
-              rv[2 * r + 1] = (unsigned)(tg << (kOzFrac - 32));
+              lv[r] = 0u;
+              rh[k] = (unsigned)(tg << (kOzFrac - 32));
             }
           }
-          tmem_st32(r_base + (unsigned)(cc * 32), rv);
+          tmem_st16(lo_base + (unsigned)(cc * 16), lv);
         }
         // This warp has read the accumulator: the MMA warp may reuse it.
         asm volatile("tcgen05.wait::st.sync.aligned;");
@@ -581,30 +574,31 @@ __global__ void __launch_bounds__(kOzThreads, 1)
         if (lane == 0) oz_abort(st, &s_abort);
         break;
       }
-      // C -= the sums: thread = one column of C, 32 of the tile's rows in
-      // chunks of 8; a warp's loads and stores of one row are 32 consecutive
-      // doubles.  Lane r holds the exponent of row r.
+      // C -= the sums: thread = one column of C, its 32 rows in chunks of 4;
+      // a warp's loads and stores of one row are 32 consecutive doubles.
+      // Lane r holds the exponent of row r.
       const int eb_j = col_ok ? eb[col] : 0;
       const int my_ea = row0 + lane < M ? ea[row0 + lane] : 0;
       double* ccol = c + (int64_t)row0 * ldc + (col_ok ? col : 0);
-#pragma unroll 1
-      for (int cc = 0; cc < 4; ++cc) {
-        unsigned rv[16];
-        tmem_ld16(r_base + (unsigned)(cc * 16), rv);
-        const double* src = ccol + (int64_t)(8 * cc) * ldc;
-        double cv[8];
 #pragma unroll
-        for (int r = 0; r < 8; ++r) cv[r] = (col_ok && row0 + 8 * cc + r < M) ? __ldcs(src + r * ldc) : 0.0;
+      for (int cc = 0; cc < 8; ++cc) {
+        unsigned lv[4];
+        tmem_ld4(lo_base + (unsigned)(cc * 4), lv);
+        double cv[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+          cv[r] = (col_ok && row0 + 4 * cc + r < M) ? __ldcs(ccol + (int64_t)(4 * cc + r) * ldc) : 0.0;
         asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
-        for (int r = 0; r < 8; ++r) {
-          const int ea_i = __shfl_sync(0xffffffffu, my_ea, 8 * cc + r);
-          cv[r] = oz_combine(rv[2 * r + 1], rv[2 * r], ea_i, eb_j, cv[r]);
+        for (int r = 0; r < 4; ++r) {
+          const int k = 4 * cc + r;
+          const int ea_i = __shfl_sync(0xffffffffu, my_ea, k);
+          cv[r] = oz_combine(rh[k], lv[r], ea_i, eb_j, cv[r]);
         }
-        double* dst = ccol + (int64_t)(8 * cc) * ldc;
 #pragma unroll
-        for (int r = 0; r < 8; ++r)
-          if (col_ok && row0 + 8 * cc + r < M) __stcs(dst + r * ldc, cv[r]);
+        for (int r = 0; r < 4; ++r)
+          if (col_ok && row0 + 4 * cc + r < M) __stcs(ccol + (int64_t)(4 * cc + r) * ldc, cv[r]);
+        asm volatile("" ::: "memory");  // keep the chunks' loads from being hoisted together
       }
     }
   }

@@ -9,9 +9,9 @@ step for step so that a GPU test can compare the kernel with it bit for bit:
 * per row of L and per column of U the exponent e of frexp(max |x|);
 * each element rounded to N = round(|x| 2^(56-e)) (ties up) and split into
   seven balanced base-256 digits, signed like x;
-* T_G = sum_{p+q=G} A_p B_q^T for G = 0..7 (integers, exact in float64 and,
+* T_G = sum_{p+q=G} A_p B_q^T for G = 0..6 (integers, exact in float64 and,
   being below 2^24, in the kernel's FP32 accumulators);
-* R = T_7 2^38, then R = T_G 2^38 + floor(R / 2^8) for G = 6..0 (int64);
+* R = T_6 2^38, then R = T_G 2^38 + floor(R / 2^8) for G = 5..0 (int64);
 * C - float64(R) 2^(ea+eb-54), NaN where a row or column held Inf or NaN.
 
 It is test infrastructure (numpy, vectorised), not a product path.
@@ -21,7 +21,7 @@ from __future__ import annotations
 import numpy as np
 
 SLICES = 7
-GROUPS = 8
+GROUPS = 7
 FRAC = 38
 NONFINITE = 1 << 20
 ZERO = -(1 << 20)
