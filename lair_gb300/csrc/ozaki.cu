@@ -293,11 +293,12 @@ __device__ __forceinline__ void oz_commit(unsigned bar) {
 
 // C - R 2^s for the fixed-point R = hi 2^32 + lo (s = ea + eb - 54); NaN
 // when a row or column held Inf or NaN.  R 2^s is rounded to 53 bits (to
-// nearest, ties to even, as a conversion of R would) and assembled with
-// 32-bit integer operations whenever it is a normal number, so the FP64 pipe
-// runs one subtraction per element; zeros, subnormal and overflowing
-// products take the general path.
-__device__ __forceinline__ double oz_combine_rare(long long R, int s, double c) {
+// nearest, ties to even, as a conversion of R would).  oz_combine_fast
+// assembles it with 32-bit integer operations whenever it is a normal number
+// and |R| >= 2^32, so the FP64 pipe runs one subtraction per element; the
+// rest (zeros, small sums, subnormal and overflowing products, non-finite
+// rows or columns) go through oz_combine, rarely.
+__device__ __noinline__ double oz_combine_rare(long long R, int s, double c) {
   const unsigned long long neg = R < 0 ? (1ull << 63) : 0ull;
   const unsigned long long u = R < 0 ? 0ull - (unsigned long long)R : (unsigned long long)R;
   if (u == 0) return __dsub_rn(c, 0.0);
@@ -326,29 +327,33 @@ __device__ __forceinline__ double oz_combine_rare(long long R, int s, double c) 
   return __dsub_rn(c, __dmul_rn(mid, p2));
 }
 
+// The common case of oz_combine: |R| >= 2^32 and a normal product.  s
+// already holds ea + eb - 54 (huge when a row or column is non-finite).
+// Returns false, leaving c alone, when the element needs oz_combine.
+__device__ __forceinline__ bool oz_combine_fast(unsigned hi, unsigned lo, int s, double& c) {
+  const unsigned sgn = (unsigned)((int)hi >> 31);  // 0 or ~0
+  // |R| = (hi, lo) negated when negative: one's complement plus one, with carry.
+  const unsigned xl = lo ^ sgn, xh = hi ^ sgn;
+  const unsigned ul = xl - sgn;
+  const unsigned uh = xh + ((sgn != 0u && ul == 0u) ? 1u : 0u);  // uh < 2^30
+  const int lz = __clz((int)uh);
+  const unsigned nh = __funnelshift_l(ul, uh, lz);  // leading one at bit 31 (when uh != 0)
+  const unsigned nl = ul << lz;
+  unsigned mh = nh >> 11, ml = __funnelshift_r(nl, nh, 11);  // 53 bits: mh has 21
+  const unsigned rem = nl & 0x7FFu;
+  const unsigned inc = (rem > 0x400u || (rem == 0x400u && (ml & 1u))) ? 1u : 0u;
+  ml += inc;
+  mh += (inc != 0u && ml == 0u) ? 1u : 0u;
+  const int E = 63 - lz + (int)(mh >> 21) + s + 1023;
+  if (uh == 0u || (unsigned)(E - 1) >= 2046u) return false;
+  const unsigned dh = (sgn & 0x80000000u) | ((unsigned)E << 20) | (mh & 0xFFFFFu);
+  c = __dsub_rn(c, __hiloint2double((int)dh, (int)ml));
+  return true;
+}
+
 __device__ __forceinline__ double oz_combine(unsigned hi, unsigned lo, int ea_i, int eb_j, double c) {
   if (ea_i >= kOzNonFinite || eb_j >= kOzNonFinite) return __longlong_as_double(0x7ff8000000000000ll);
-  const int s = ea_i + eb_j - (kOzFrac + 16);
-  // Common case: |R| >= 2^32 (hi carries the leading one), result normal.
-  const bool neg = (int)hi < 0;
-  const unsigned ul = neg ? 0u - lo : lo;
-  const unsigned uh = neg ? ~hi + (lo == 0u ? 1u : 0u) : hi;  // |R| = uh 2^32 + ul, uh < 2^30
-  const int lz = __clz((int)uh);                              // 2 .. 32
-  if (uh != 0u) {
-    const unsigned nh = __funnelshift_l(ul, uh, lz);  // leading one at bit 31
-    const unsigned nl = ul << lz;
-    unsigned mh = nh >> 11, ml = __funnelshift_r(nl, nh, 11);  // 53 bits: mh has 21
-    const unsigned rem = nl & 0x7FFu;
-    const unsigned inc = (rem > 0x400u || (rem == 0x400u && (ml & 1u))) ? 1u : 0u;
-    ml += inc;
-    mh += (inc & (ml == 0u ? 1u : 0u));
-    const int E = 63 - lz + (int)(mh >> 21) + s + 1023;
-    if (E >= 1 && E <= 2046) {
-      const unsigned dh = (neg ? 0x80000000u : 0u) | ((unsigned)E << 20) | (mh & 0xFFFFFu);
-      return __dsub_rn(c, __hiloint2double((int)dh, (int)ml));
-    }
-  }
-  return oz_combine_rare((long long)(((unsigned long long)hi << 32) | lo), s, c);
+  return oz_combine_rare((long long)(((unsigned long long)hi << 32) | lo), ea_i + eb_j - (kOzFrac + 16), c);
 }
 
 __global__ void __launch_bounds__(kOzThreads, 1)
@@ -541,28 +546,39 @@ __global__ void __launch_bounds__(kOzThreads, 1)
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;");
+        const unsigned acc = lane_base + (unsigned)(buf * kOzBM + rq * 32);
+        if (G == kOzGroups - 1) {
+          // First group: R = T 2^38.
 #pragma unroll
-        for (int cc = 0; cc < 2; ++cc) {
-          unsigned tv[16], lv[16];
-          tmem_ld16(lane_base + (unsigned)(buf * kOzBM + rq * 32 + cc * 16), tv);
-          if (G < kOzGroups - 1) tmem_ld16(lo_base + (unsigned)(cc * 16), lv);
-          asm volatile("tcgen05.wait::ld.sync.aligned;");
+          for (int cc = 0; cc < 2; ++cc) {
+            unsigned tv[16], lv[16];
+            tmem_ld16(acc + (unsigned)(cc * 16), tv);
+            asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+            for (int r = 0; r < 16; ++r) {
+              rh[cc * 16 + r] = (unsigned)(__float2int_rn(__uint_as_float(tv[r])) << (kOzFrac - 32));
+              lv[r] = 0u;
+            }
+            tmem_st16(lo_base + (unsigned)(cc * 16), lv);
+          }
+        } else {
           // R = T 2^38 + floor(R / 2^8) on (hi, lo) words: T 2^38 only
           // touches hi (|R| < 2^62), so no carry crosses the words.
 #pragma unroll
-          for (int r = 0; r < 16; ++r) {
-            const int k = cc * 16 + r;
-            const int tg = __float2int_rn(__uint_as_float(tv[r]));
-            if (G < kOzGroups - 1) {
-              const unsigned hi = rh[k];
+          for (int cc = 0; cc < 2; ++cc) {
+            unsigned tv[16], lv[16];
+            tmem_ld16(acc + (unsigned)(cc * 16), tv);
+            tmem_ld16(lo_base + (unsigned)(cc * 16), lv);
+            asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+            for (int r = 0; r < 16; ++r) {
+              const unsigned hi = rh[cc * 16 + r];
               lv[r] = __funnelshift_r(lv[r], hi, 8);
-              rh[k] = (unsigned)(((int)hi >> 8) + (tg << (kOzFrac - 32)));
-            } else {
-              lv[r] = 0u;
-              rh[k] = (unsigned)(tg << (kOzFrac - 32));
+              rh[cc * 16 + r] =
+                  (unsigned)(((int)hi >> 8) + (__float2int_rn(__uint_as_float(tv[r])) << (kOzFrac - 32)));
             }
+            tmem_st16(lo_base + (unsigned)(cc * 16), lv);
           }
-          tmem_st16(lo_base + (unsigned)(cc * 16), lv);
         }
         // This warp has read the accumulator: the MMA warp may reuse it.
         asm volatile("tcgen05.wait::st.sync.aligned;");
@@ -576,28 +592,52 @@ __global__ void __launch_bounds__(kOzThreads, 1)
       }
       // C -= the sums: thread = one column of C, its 32 rows in chunks of 4;
       // a warp's loads and stores of one row are 32 consecutive doubles.
-      // Lane r holds the exponent of row r.
+      // Lane r holds the exponent of row r.  Elements the fast path declines
+      // (rare) are redone, warp-uniformly, by the general path.
       const int eb_j = col_ok ? eb[col] : 0;
       const int my_ea = row0 + lane < M ? ea[row0 + lane] : 0;
-      double* ccol = c + (int64_t)row0 * ldc + (col_ok ? col : 0);
+      const int s_col = eb_j >= kOzNonFinite ? (1 << 24) : eb_j - (kOzFrac + 16);
+      const int s_row = my_ea >= kOzNonFinite ? (1 << 24) : my_ea;
+      const bool whole = (jb * kOzBN + quarter * 32 + 32 <= N) && (row0 + 32 <= M);  // warp-uniform
+      double* cptr = c + (int64_t)row0 * ldc + (col_ok ? col : 0);
 #pragma unroll
       for (int cc = 0; cc < 8; ++cc) {
         unsigned lv[4];
         tmem_ld4(lo_base + (unsigned)(cc * 4), lv);
         double cv[4];
+        if (whole) {
 #pragma unroll
-        for (int r = 0; r < 4; ++r)
-          cv[r] = (col_ok && row0 + 4 * cc + r < M) ? __ldcs(ccol + (int64_t)(4 * cc + r) * ldc) : 0.0;
+          for (int r = 0; r < 4; ++r) cv[r] = __ldcs(cptr + (int64_t)r * ldc);
+        } else {
+#pragma unroll
+          for (int r = 0; r < 4; ++r)
+            cv[r] = (col_ok && row0 + 4 * cc + r < M) ? __ldcs(cptr + (int64_t)r * ldc) : 0.0;
+        }
         asm volatile("tcgen05.wait::ld.sync.aligned;");
+        unsigned declined = 0;
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
           const int k = 4 * cc + r;
-          const int ea_i = __shfl_sync(0xffffffffu, my_ea, k);
-          cv[r] = oz_combine(rh[k], lv[r], ea_i, eb_j, cv[r]);
+          const int s = s_col + __shfl_sync(0xffffffffu, s_row, k);
+          if (!oz_combine_fast(rh[k], lv[r], s, cv[r])) declined |= 1u << r;
         }
+        if (__any_sync(0xffffffffu, declined != 0u)) {
 #pragma unroll
-        for (int r = 0; r < 4; ++r)
-          if (col_ok && row0 + 4 * cc + r < M) __stcs(ccol + (int64_t)(4 * cc + r) * ldc, cv[r]);
+          for (int r = 0; r < 4; ++r) {
+            const int k = 4 * cc + r;
+            const int ea_i = __shfl_sync(0xffffffffu, my_ea, k);
+            if (declined & (1u << r)) cv[r] = oz_combine(rh[k], lv[r], ea_i, eb_j, cv[r]);
+          }
+        }
+        if (whole) {
+#pragma unroll
+          for (int r = 0; r < 4; ++r) __stcs(cptr + (int64_t)r * ldc, cv[r]);
+        } else {
+#pragma unroll
+          for (int r = 0; r < 4; ++r)
+            if (col_ok && row0 + 4 * cc + r < M) __stcs(cptr + (int64_t)r * ldc, cv[r]);
+        }
+        cptr += 4 * ldc;
         asm volatile("" ::: "memory");  // keep the chunks' loads from being hoisted together
       }
     }
