@@ -1176,14 +1176,30 @@ static int launch_laswp(luhot_ctx* ctx, T* a, int64_t lda, int k0, int w, int n,
   return LUHOT_OK;
 }
 
+// The tensor-core engine takes the U12 solve of fast-mode FP64 as well
+// (ozaki_trsm: U12 = A12 - (I - L11^-1) A12) for at least 256 columns (128
+// with LUHOT_UPDATE_OZAKI), when the trailing update runs on it.
+static bool trsm_on_slices(const void* oz_ws, int engine, int ncols) {
+  if (!oz_ws || engine == LUHOT_UPDATE_DMMA) return false;
+  return ncols >= (engine == LUHOT_UPDATE_OZAKI ? 128 : 256);
+}
+
 // U12 = L11^-1 A12 for the panel [k0, k0 + w): rows [k0, k0 + w) of the
 // columns [c_begin, c_end).
 template <typename T, bool kExact>
 static int launch_trsm(luhot_ctx* ctx, T* a, int64_t lda, int k0, int w, int c_begin, int c_end,
-                       cudaStream_t stream) {
+                       cudaStream_t stream, void* oz_ws = nullptr, int engine = LUHOT_UPDATE_DMMA) {
   if (c_begin >= c_end) return LUHOT_OK;
   const int tgrid = (c_end - c_begin + kTrsmCols - 1) / kTrsmCols;
   prof_begin(ctx, kProfTrsm);
+  if constexpr (std::is_same<T, double>::value && !kExact) {
+    if (w <= 64 && trsm_on_slices(oz_ws, engine, c_end - c_begin)) {
+      const int rc = ozaki_trsm(ctx, a, lda, k0, w, c_begin, c_end, oz_ws, stream);
+      prof_end(ctx, kProfTrsm, (double)w * (w - 1) * (c_end - c_begin),
+               ((double)w * w + 2.0 * w * (c_end - c_begin)) * sizeof(T));
+      return rc;
+    }
+  }
   if (!kExact && w <= 64) {
     const size_t smem = ((size_t)64 * 64 + (size_t)64 * kTrsmCols) * sizeof(T);
     LUHOT_CUDA_TRY(ctx, allow_max_dynamic_smem(trsm_fast_kernel<T, 64>));
@@ -1255,7 +1271,7 @@ static int getrf_impl(luhot_ctx* ctx, int m, int n, T* a, int64_t lda, int* piv,
     if (rc) return rc;
     const int c_right = k0 + w;
     if (c_right < n) {
-      rc = launch_trsm<T, kExact>(ctx, a, lda, k0, w, c_right, n, stream);
+      rc = launch_trsm<T, kExact>(ctx, a, lda, k0, w, c_right, n, stream, oz_ws, ctx->fp64_update);
       if (!rc) rc = schur_update<T, kExact>(ctx, a, lda, k0, w, m, n, oz_ws, ctx->fp64_update, stream);
       if (rc) return rc;
     }

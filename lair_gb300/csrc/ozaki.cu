@@ -202,6 +202,42 @@ __global__ void __launch_bounds__(256) oz_split_cols_kernel(const double* __rest
   }
 }
 
+// U12 = L11^-1 A12 as a product: U12 = A12 - N A12 with N = I - L11^-1
+// (strictly lower).  oz_trsm_inverse_kernel forms N for the unit lower
+// triangular L11 = a[k0.., k0..] (w x w, w <= 64) into nb (128 x 64,
+// row-major; rows >= w and columns >= w zero), one CTA per column c: warp 0
+// holds x = L11^-1 e_c (rows lane and lane + 32) and runs the column sweep
+// x_i -= L(i,k) x_k for i > k, k = c, c + 1, ... (x_k by shuffle), so each
+// step costs one shuffle and two FMAs on this part's thin FP64 pipe; the
+// CTA's four warps first stage L11 in shared memory.  oz_split_rows_kernel
+// then writes N's digit slices like any L21.
+constexpr int kOzInvLds = 65;
+constexpr int kOzMapRows = 128;  // rows of the L-slice tensor map of the triangular solve
+
+__global__ void __launch_bounds__(128) oz_trsm_inverse_kernel(const double* __restrict__ a, int64_t lda, int k0, int w,
+                                                              double* __restrict__ nb) {
+  __shared__ double L[kOzK * kOzInvLds];  // L[i * kOzInvLds + k] = L11(i, k) for k < i < w, else 0
+  const int c = blockIdx.x, tid = threadIdx.x;
+  for (int idx = tid; idx < kOzK * kOzK; idx += blockDim.x) {
+    const int i = idx >> 6, k = idx & 63;
+    L[i * kOzInvLds + k] = (i < w && k < i && k >= c) ? a[(int64_t)(k0 + i) * lda + k0 + k] : 0.0;
+  }
+  __syncthreads();
+  if (tid >= 32) return;
+  const int lane = tid;
+  double x0 = lane == c ? 1.0 : 0.0, x1 = lane + 32 == c ? 1.0 : 0.0;
+  for (int k = c; k < w - 1; ++k) {
+    const double xk = __shfl_sync(0xffffffffu, k < 32 ? x0 : x1, k & 31);
+    if (lane > k) x0 = fma(-L[lane * kOzInvLds + k], xk, x0);
+    if (lane + 32 > k) x1 = fma(-L[(lane + 32) * kOzInvLds + k], xk, x1);
+  }
+  // N(i, c) = -x_i below the diagonal (the unit diagonal cancels), zero elsewhere
+  nb[lane * kOzK + c] = (lane > c && lane < w && c < w) ? -x0 : 0.0;
+  nb[(lane + 32) * kOzK + c] = (lane + 32 > c && lane + 32 < w && c < w) ? -x1 : 0.0;
+  nb[(lane + 64) * kOzK + c] = 0.0;
+  nb[(lane + 96) * kOzK + c] = 0.0;
+}
+
 // ---------------------------------------------------------------------------
 // Products and combine.
 // ---------------------------------------------------------------------------
@@ -664,9 +700,36 @@ __global__ void __launch_bounds__(kOzThreads, 1)
 // ---------------------------------------------------------------------------
 static size_t oz_round(size_t b) { return (b + 1023) / 1024 * 1024; }
 
+// Workspace layout for an M x N product: A slices [7][M'][64], B slices
+// [7][N][64], exponents ea[M'], eb[N], with M' = max(M, 128) (the triangular
+// solve's L slices always have 128 rows).
+struct OzWs {
+  __half* as;
+  __half* bs;
+  int* ea;
+  int* eb;
+  double* nb;  // N = I - L11^-1 of the triangular solve (128 x 64)
+};
+static OzWs oz_layout(void* ws, int M, int N) {
+  const size_t Mp = (size_t)std::max(M, kOzMapRows);
+  char* p = static_cast<char*>(ws);
+  OzWs w;
+  w.as = reinterpret_cast<__half*>(p);
+  p += oz_round((size_t)kOzSlices * Mp * kOzK * 2);
+  w.bs = reinterpret_cast<__half*>(p);
+  p += oz_round((size_t)kOzSlices * N * kOzK * 2);
+  w.ea = reinterpret_cast<int*>(p);
+  p += oz_round(Mp * 4);
+  w.eb = reinterpret_cast<int*>(p);
+  p += oz_round((size_t)N * 4);
+  w.nb = reinterpret_cast<double*>(p);
+  return w;
+}
+
 size_t ozaki_workspace_bytes(int m, int n) {
-  return oz_round((size_t)kOzSlices * m * kOzK * 2) + oz_round((size_t)kOzSlices * n * kOzK * 2) +
-         oz_round((size_t)m * 4) + oz_round((size_t)n * 4);
+  const size_t mp = (size_t)std::max(m, kOzMapRows);
+  return oz_round((size_t)kOzSlices * mp * kOzK * 2) + oz_round((size_t)kOzSlices * n * kOzK * 2) + oz_round(mp * 4) +
+         oz_round((size_t)n * 4) + oz_round((size_t)kOzMapRows * kOzK * sizeof(double));
 }
 
 bool ozaki_available(luhot_ctx* ctx) { return kOzSmem <= (size_t)ctx->max_smem_optin && encode_fn() != nullptr; }
@@ -688,6 +751,22 @@ static int make_slice_map(luhot_ctx* ctx, CUtensorMap* map, void* ptr, int rows,
   return LUHOT_OK;
 }
 
+// C (M x N, ldc) -= the product of the slices in `w` (L map of map_rows
+// rows); one persistent launch.
+static int oz_launch_gemm(luhot_ctx* ctx, const OzWs& w, int map_rows, double* c, int64_t ldc, int M, int N,
+                          cudaStream_t stream) {
+  CUtensorMap tmL, tmU;
+  int rc = make_slice_map(ctx, &tmL, w.as, map_rows, kOzBM);
+  if (!rc) rc = make_slice_map(ctx, &tmU, w.bs, N, kOzBN);
+  if (rc) return rc;
+  const int tiles = ((M + kOzBM - 1) / kOzBM) * ((N + kOzBN - 1) / kOzBN);
+  LUHOT_CUDA_TRY(ctx, allow_max_dynamic_smem(oz_gemm_kernel));
+  oz_gemm_kernel<<<std::min(tiles, ctx->num_sms), kOzThreads, kOzSmem, stream>>>(tmL, tmU, c, ldc, M, N, w.ea, w.eb,
+                                                                                ctx->d_status);
+  LUHOT_CUDA_TRY(ctx, cudaGetLastError());
+  return LUHOT_OK;
+}
+
 int ozaki_update(luhot_ctx* ctx, double* a, int64_t lda, int k0, int w, int r1, int m, int c1, int n, void* ws,
                  cudaStream_t stream) {
   const int M = m - r1, N = n - c1;
@@ -697,38 +776,35 @@ int ozaki_update(luhot_ctx* ctx, double* a, int64_t lda, int k0, int w, int r1, 
     if (rc) return rc;
     return ozaki_update(ctx, a, lda, k0 + kOzK, w - kOzK, r1, m, c1, n, ws, stream);
   }
-  char* p = static_cast<char*>(ws);
-  __half* as = reinterpret_cast<__half*>(p);
-  p += oz_round((size_t)kOzSlices * M * kOzK * 2);
-  __half* bs = reinterpret_cast<__half*>(p);
-  p += oz_round((size_t)kOzSlices * N * kOzK * 2);
-  int* ea = reinterpret_cast<int*>(p);
-  p += oz_round((size_t)M * 4);
-  int* eb = reinterpret_cast<int*>(p);
+  const OzWs lay = oz_layout(ws, M, N);
 
   prof_begin(ctx, kProfOther);
-  oz_split_rows_kernel<<<(M + 7) / 8, 256, 0, stream>>>(a, lda, r1, M, k0, w, as, ea);
+  oz_split_rows_kernel<<<(M + 7) / 8, 256, 0, stream>>>(a, lda, r1, M, k0, w, lay.as, lay.ea);
   prof_end(ctx, kProfOther, 0.0, (double)M * w * 8 + (double)M * kOzK * kOzSlices * 2);
   prof_begin(ctx, kProfOther);
-  oz_split_cols_kernel<<<(N + 31) / 32, 256, 0, stream>>>(a, lda, k0, w, c1, N, bs, eb);
+  oz_split_cols_kernel<<<(N + 31) / 32, 256, 0, stream>>>(a, lda, k0, w, c1, N, lay.bs, lay.eb);
   prof_end(ctx, kProfOther, 0.0, (double)N * w * 8 + (double)N * kOzK * kOzSlices * 2);
   LUHOT_CUDA_TRY(ctx, cudaGetLastError());
 
-  CUtensorMap tmL, tmU;
-  int rc = make_slice_map(ctx, &tmL, as, M, kOzBM);
-  if (!rc) rc = make_slice_map(ctx, &tmU, bs, N, kOzBN);
-  if (rc) return rc;
-  double* cb = a + (int64_t)r1 * lda + c1;
-  const int tiles = ((M + kOzBM - 1) / kOzBM) * ((N + kOzBN - 1) / kOzBN);
-  LUHOT_CUDA_TRY(ctx, allow_max_dynamic_smem(oz_gemm_kernel));
   prof_begin(ctx, kProfGemm);
-  oz_gemm_kernel<<<std::min(tiles, ctx->num_sms), kOzThreads, kOzSmem, stream>>>(tmL, tmU, cb, lda, M, N, ea, eb,
-                                                                                ctx->d_status);
+  int rc = oz_launch_gemm(ctx, lay, M, a + (int64_t)r1 * lda + c1, lda, M, N, stream);
   // algorithmic work: 2MNK FP64 flops; bytes: C read + written, the slices read once
   prof_end(ctx, kProfGemm, 2.0 * M * N * w,
            (double)M * N * 16 + (double)(M + N) * kOzK * kOzSlices * 2 + (double)(M + N) * 4);
+  return rc;
+}
+
+int ozaki_trsm(luhot_ctx* ctx, double* a, int64_t lda, int k0, int w, int c1, int n, void* ws, cudaStream_t stream) {
+  const int N = n - c1;
+  if (N <= 0 || w <= 1) return LUHOT_OK;
+  if (w > kOzK || N < kOzBN) return set_error(ctx, LUHOT_ERR_INVALID_ARG, "ozaki_trsm: w > 64 or fewer than 128 columns");
+  const OzWs lay = oz_layout(ws, w, N);
+  oz_trsm_inverse_kernel<<<kOzK, 128, 0, stream>>>(a, lda, k0, w, lay.nb);
+  oz_split_rows_kernel<<<kOzMapRows / 8, 256, 0, stream>>>(lay.nb, kOzK, 0, kOzMapRows, 0, w, lay.as, lay.ea);
+  oz_split_cols_kernel<<<(N + 31) / 32, 256, 0, stream>>>(a, lda, k0, w, c1, N, lay.bs, lay.eb);
   LUHOT_CUDA_TRY(ctx, cudaGetLastError());
-  return LUHOT_OK;
+  // rows [k0, k0 + w) of columns [c1, n): A12 -= N A12 (its slices were taken first)
+  return oz_launch_gemm(ctx, lay, kOzMapRows, a + (int64_t)k0 * lda + c1, lda, w, N, stream);
 }
 
 }  // namespace luhot

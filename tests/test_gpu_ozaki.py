@@ -113,3 +113,37 @@ def test_getrf_ozaki_matches_dmma(n):
     berr = np.abs(pa - lo @ up).max() / (n * np.finfo(float).eps * np.abs(a0).max())
     print(f"\nn={n}: max|PA - LU| / (n eps max|A|) = {berr:.3f}")
     assert berr < 1.0
+
+
+@pytest.mark.parametrize("m,n", [(300, 2000), (1000, 1000), (2000, 300)])
+def test_getrf_triangular_solves_on_slices(m, n):
+    """With the tensor-core engine the U12 solves of fast-mode FP64 getrf run
+    as U12 = A12 - (I - L11^-1) A12 on the FP16 slice products (from 128
+    columns with LUHOT_UPDATE_OZAKI, 256 with the default engine).  Wide,
+    square and tall shapes: the pivots equal the DMMA engine's (whose solves
+    are FMA substitutions), the factors agree to 1e-11 of max |LU| and
+    max |PA - LU| stays below n eps max |A|."""
+    rng = np.random.default_rng(m * 13 + n)
+    a0 = rng.standard_normal((m, n))
+    outs = {}
+    try:
+        for engine in ("dmma", "ozaki", "auto"):
+            _lib.set_fp64_update(engine)
+            a = a0.copy()
+            piv, sing = lapack.getrf(a, mode="fast")
+            outs[engine] = (a, piv, sing)
+    finally:
+        _lib.set_fp64_update("auto")
+    a_d, piv_d, sing_d = outs["dmma"]
+    k = min(m, n)
+    for engine in ("ozaki", "auto"):
+        a_o, piv_o, sing_o = outs[engine]
+        assert piv_o == piv_d and sing_o == sing_d
+        assert np.abs(a_o - a_d).max() <= 1e-11 * np.abs(a_d).max()
+        lo = np.tril(a_o, -1)[:, :k] + np.eye(m, k)
+        up = np.triu(a_o)[:k, :]
+        pa = a0.copy()
+        for i, p in enumerate(piv_o):
+            pa[[i, p]] = pa[[p, i]]
+        err = np.abs(pa - lo @ up).max() / (max(m, n) * np.finfo(float).eps * np.abs(a0).max())
+        assert err < 1.0, (engine, err)
