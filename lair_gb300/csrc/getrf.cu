@@ -1079,13 +1079,15 @@ static int launch_panel(luhot_ctx* ctx, T* a, int64_t lda, int m, int k0, int w,
   cudaFuncAttributes fa;
   LUHOT_CUDA_TRY(ctx, cudaFuncGetAttributes(&fa, kern));
   const int max_smem = ctx->max_smem_optin - (int)fa.sharedSizeBytes;  // less the static exchange buffers
-  // CTAs: enough that each owns >= 32 rows, at most pmax (raised up to the
-  // SM count when the rows of one CTA would not fit in shared memory).
-  // The exchange latency per column grows with P; FP32 panels (whose
-  // update work is light) run fastest on 64 CTAs, FP64 panels need the
-  // FP64 pipes of every SM.
-  const int pmax = sizeof(T) == 4 ? std::min(ctx->num_sms, 64) : ctx->num_sms;
-  int P = std::min(pmax, std::max(1, (rows + 31) / 32));
+  // CTAs: FP32 panels (light update work) run fastest on 64 CTAs with >= 32
+  // rows each; FP64 panels, whose look-ahead update needs FP64 pipes, on 96
+  // CTAs with >= 64 rows each (measured at n = 16384 against 64 .. 152 CTAs:
+  // fewer CTAs shorten the per-column exchange, more share the update).  The
+  // count is raised, up to the SM count, when the rows of one CTA would not
+  // fit in shared memory.
+  const int pmax = std::min(ctx->num_sms, sizeof(T) == 4 ? 64 : 96);
+  const int min_rows = sizeof(T) == 4 ? 32 : 64;
+  int P = std::min(pmax, std::max(1, (rows + min_rows - 1) / min_rows));
   int rows_per = (rows + P - 1) / P;
   while (panel_smem_bytes<T>(rows_per, w) > (size_t)max_smem && P < ctx->num_sms) {
     P = std::min(ctx->num_sms, P * 2);

@@ -224,10 +224,11 @@ int getrs_perm(luhot_ctx* ctx, const int* piv, int n, int* perm) {
 
 int trsv_scratch(luhot_ctx* ctx, int n, int** flags, int** ticket) {
   const int nblk = trsv_syncfree_blocks(n);
-  int rc = ensure_buf(ctx, ctx->trsv_buf, ((size_t)nblk + 64) * sizeof(int));
+  // ready flags of up to four chains of right-hand sides, then the ticket
+  int rc = ensure_buf(ctx, ctx->trsv_buf, (4 * (size_t)nblk + 64) * sizeof(int));
   if (rc) return rc;
   *flags = static_cast<int*>(ctx->trsv_buf.ptr);
-  *ticket = *flags + ((nblk + 31) / 32) * 32;
+  *ticket = *flags + ((4 * nblk + 31) / 32) * 32;
   return LUHOT_OK;
 }
 

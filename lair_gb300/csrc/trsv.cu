@@ -133,8 +133,8 @@ __device__ __forceinline__ bool wait_ready(const int* flags, int j, DeviceStatus
 // kNR: right-hand sides handled per launch (1, 2, 4 or 16; runtime nrhs <= kNR).
 template <typename T, typename TA, bool kExact, bool kLower, bool kUnit, bool kTrans, int kNR>
 __global__ void __launch_bounds__(kThreads) trsv_syncfree_kernel(const TA* __restrict__ a, int64_t lda, T* x,
-                                                                 int64_t ldx, int n, int nrhs, int* flags,
-                                                                 int* ticket, DeviceStatus* st,
+                                                                 int64_t ldx, int n, int nrhs, int nchain,
+                                                                 int* flags, int* ticket, DeviceStatus* st,
                                                                  const T* __restrict__ dinv) {
   // Threads per (row, rhs) pair: k split only in fast mode.
   constexpr int kKS = kExact ? 1 : (kNR >= 4 ? 1 : 4 / kNR);
@@ -152,8 +152,14 @@ __global__ void __launch_bounds__(kThreads) trsv_syncfree_kernel(const TA* __res
   const int nblk = (n + kBS - 1) / kBS;
   if (threadIdx.x == 0) s_ticket = atomicAdd(ticket, 1);
   __syncthreads();
-  const int t = s_ticket;
-  if (t >= nblk) return;
+  // Ticket -> (chain, block): the chains (groups of kNR right-hand sides)
+  // advance together, and a block of any chain only waits for blocks of its
+  // own chain with smaller tickets.
+  if (s_ticket >= nblk * nchain) return;
+  const int chain = s_ticket % nchain, t = s_ticket / nchain;
+  x += chain * kNR;
+  nrhs = min(kNR, nrhs - chain * kNR);
+  flags += (size_t)chain * nblk;
   const int I = kLower ? t : (nblk - 1 - t);
   const int i0 = I * kBS;
   const int rows = min(kBS, n - i0);
@@ -351,23 +357,30 @@ __global__ void __launch_bounds__(kThreads) trsv_syncfree_kernel(const TA* __res
 size_t trsv_syncfree_smem(size_t elem) { return (2 * (size_t)kBS * kLds + 2 * (size_t)kBS * kMaxRhs) * elem; }
 int trsv_syncfree_blocks(int n) { return (n + kBS - 1) / kBS; }
 
+// Fast sweeps of more than four right-hand sides run as independent chains
+// of four (one launch): each chain step (the last off-diagonal tile and the
+// diagonal block of a 64-row block) is then a quarter of the FP64 work on
+// the critical path of one chain of sixteen.
+static int trsv_chains(bool exact, int nc) { return (!exact && nc > 4) ? (nc + 3) / 4 : 1; }
+
 template <typename T, typename TA, bool EX, bool LO, bool UN, bool TR>
 static cudaError_t launch_case(cudaStream_t stream, const TA* a, int64_t lda, T* x, int64_t ldx, int n, int nc,
                                int* flags, int* ticket, DeviceStatus* st, const T* dinv) {
   const int nblk = trsv_syncfree_blocks(n);
   const size_t smem = trsv_syncfree_smem(sizeof(T));
+  const int nchain = trsv_chains(EX, nc);
   cudaError_t e;
-#define LUHOT_TRSV_NR(NR)                                                                       \
-  {                                                                                             \
-    auto k = trsv_syncfree_kernel<T, TA, EX, LO, UN, TR, NR>;                                   \
-    e = allow_max_dynamic_smem(k);                                                              \
-    if (e != cudaSuccess) return e;                                                             \
-    k<<<nblk, kThreads, smem, stream>>>(a, lda, x, ldx, n, nc, flags, ticket, st, dinv);        \
-    return cudaGetLastError();                                                                  \
+#define LUHOT_TRSV_NR(NR)                                                                                \
+  {                                                                                                      \
+    auto k = trsv_syncfree_kernel<T, TA, EX, LO, UN, TR, NR>;                                            \
+    e = allow_max_dynamic_smem(k);                                                                       \
+    if (e != cudaSuccess) return e;                                                                      \
+    k<<<nblk * nchain, kThreads, smem, stream>>>(a, lda, x, ldx, n, nc, nchain, flags, ticket, st, dinv); \
+    return cudaGetLastError();                                                                           \
   }
   if (nc == 1) LUHOT_TRSV_NR(1)
   if (nc == 2) LUHOT_TRSV_NR(2)
-  if (nc <= 4) LUHOT_TRSV_NR(4)
+  if (nc <= 4 || nchain > 1) LUHOT_TRSV_NR(4)
   LUHOT_TRSV_NR(16)
 #undef LUHOT_TRSV_NR
 }
@@ -381,7 +394,7 @@ cudaError_t launch_trsv_syncfree(cudaStream_t stream, const TA* a, int64_t lda, 
   if (exact) dinv = nullptr;  // inverses serve the fast sweeps only
   for (int c0 = 0; c0 < nrhs; c0 += kMaxRhs) {
     const int nc = std::min(kMaxRhs, nrhs - c0);
-    cudaError_t e = cudaMemsetAsync(flags, 0, (size_t)nblk * sizeof(int), stream);
+    cudaError_t e = cudaMemsetAsync(flags, 0, (size_t)nblk * trsv_chains(exact, nc) * sizeof(int), stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(ticket, 0, sizeof(int), stream);
     if (e != cudaSuccess) return e;
     T* xc = x + c0;

@@ -13,7 +13,7 @@ size_t trsv_syncfree_smem(size_t elem_bytes);
 int trsv_syncfree_blocks(int n);
 
 // op(A) x = b in place for nrhs columns of x (row-major, ldx); flags must hold
-// trsv_syncfree_blocks(n) ints and ticket one int of device scratch (both
+// 4 * trsv_syncfree_blocks(n) ints and ticket one int of device scratch (both
 // cleared by this call); st supplies the wait limit and records a timeout.
 // TA is the storage type of the factor (it may be narrower than T).  dinv,
 // when not null, holds the inverses of the 64 x 64 diagonal blocks of the
