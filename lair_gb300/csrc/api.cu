@@ -508,6 +508,11 @@ void luhot_destroy(luhot_ctx* ctx) {
   if (ctx->chain_buf.ptr) cudaFree(ctx->chain_buf.ptr);
   if (ctx->scaled_buf.ptr) cudaFree(ctx->scaled_buf.ptr);
   if (ctx->oz_buf.ptr) cudaFree(ctx->oz_buf.ptr);
+  if (ctx->la_moves.ptr) cudaFree(ctx->la_moves.ptr);
+  for (auto& e : ctx->la_ev)
+    if (e) cudaEventDestroy(e);
+  if (ctx->la_hi) cudaStreamDestroy(ctx->la_hi);
+  if (ctx->la_lo) cudaStreamDestroy(ctx->la_lo);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
 }

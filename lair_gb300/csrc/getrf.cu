@@ -664,8 +664,8 @@ __global__ void __launch_bounds__(512, 1) panel_kernel(PanelArgs<T> p) {
 //    segments.  Pure data movement, so exact mode is unaffected.
 template <typename T>
 __global__ void __launch_bounds__(256) laswp_moves_kernel(T* a, int64_t lda, const int* moves,
-                                                          const int* move_count, int capacity, int c_left_end,
-                                                          int c_right_begin, int n) {
+                                                          const int* move_count, int capacity, int c_left_begin,
+                                                          int c_left_end, int c_right_begin, int n) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* vals = reinterpret_cast<T*>(smem_raw);  // [capacity][32]
   __shared__ int mv[4 * kMaxPanelWidth];      // the (destination, source) pairs
@@ -673,11 +673,11 @@ __global__ void __launch_bounds__(256) laswp_moves_kernel(T* a, int64_t lda, con
   const int tid = threadIdx.y * 32 + threadIdx.x;
   for (int i = tid; i < 2 * count; i += blockDim.x * blockDim.y) mv[i] = moves[i];
   __syncthreads();
-  const int nleft = c_left_end;
+  const int nleft = max(0, c_left_end - c_left_begin);
   const int t = blockIdx.x * 32 + threadIdx.x;
   const int nright = max(0, n - c_right_begin);
   const bool on = t < nleft + nright;
-  const int c = (t < nleft) ? t : (c_right_begin + t - nleft);
+  const int c = (t < nleft) ? (c_left_begin + t) : (c_right_begin + t - nleft);
   // Eight source rows per thread in flight before any is stored.
   constexpr int kB = 8;
   for (int e0 = threadIdx.y; e0 < count; e0 += blockDim.y * kB) {
@@ -1160,22 +1160,30 @@ static int launch_gemm(luhot_ctx* ctx, T* a, int64_t lda, int r0, int c0, int kk
   return LUHOT_OK;
 }
 
+// Row interchanges of a panel of width w, from the list of moved rows it
+// reported (`moves`: kPanelMovesBytes, the layout of the panel scratch), on
+// the columns [cl0, cl1) and [cr0, cr1).
+template <typename T>
+static int launch_laswp_cols(luhot_ctx* ctx, T* a, int64_t lda, const int* moves, int w, int cl0, int cl1, int cr0,
+                             int cr1, cudaStream_t stream) {
+  const int ncols_swap = std::max(0, cl1 - cl0) + std::max(0, cr1 - cr0);
+  if (ncols_swap <= 0) return LUHOT_OK;
+  prof_begin(ctx, kProfLaswp);
+  const size_t lsm = (size_t)2 * w * 32 * sizeof(T);
+  LUHOT_CUDA_TRY(ctx, allow_max_dynamic_smem(laswp_moves_kernel<T>));
+  laswp_moves_kernel<T><<<(ncols_swap + 31) / 32, dim3(32, 8), lsm, stream>>>(
+      a, lda, moves, moves + 4 * kMaxPanelWidth, 2 * w, cl0, std::max(cl0, cl1), cr0, std::max(cr0, cr1));
+  prof_end(ctx, kProfLaswp, 0.0, 4.0 * w * ncols_swap * sizeof(T));
+  LUHOT_CUDA_TRY(ctx, cudaGetLastError());
+  return LUHOT_OK;
+}
+
 // Row interchanges of the panel [k0, k0 + w) (the moves it reported) on every
 // column outside the panel: [0, k0) and [k0 + w, n).
 template <typename T>
 static int launch_laswp(luhot_ctx* ctx, T* a, int64_t lda, int k0, int w, int n, cudaStream_t stream) {
-  const int c_right = k0 + w;
-  const int ncols_swap = k0 + std::max(0, n - c_right);
-  if (ncols_swap <= 0) return LUHOT_OK;
-  prof_begin(ctx, kProfLaswp);
-  int* moves = reinterpret_cast<int*>(static_cast<char*>(ctx->panel_scratch) + kPanelSlotBytes);
-  const size_t lsm = (size_t)2 * w * 32 * sizeof(T);
-  LUHOT_CUDA_TRY(ctx, allow_max_dynamic_smem(laswp_moves_kernel<T>));
-  laswp_moves_kernel<T><<<(ncols_swap + 31) / 32, dim3(32, 8), lsm, stream>>>(
-      a, lda, moves, moves + 4 * kMaxPanelWidth, 2 * w, k0, c_right, n);
-  prof_end(ctx, kProfLaswp, 0.0, 4.0 * w * ncols_swap * sizeof(T));
-  LUHOT_CUDA_TRY(ctx, cudaGetLastError());
-  return LUHOT_OK;
+  const int* moves = reinterpret_cast<const int*>(static_cast<char*>(ctx->panel_scratch) + kPanelSlotBytes);
+  return launch_laswp_cols<T>(ctx, a, lda, moves, w, 0, k0, k0 + w, n, stream);
 }
 
 // The tensor-core engine takes the U12 solve of fast-mode FP64 as well
@@ -1283,43 +1291,137 @@ static int getrf_impl(luhot_ctx* ctx, int m, int n, T* a, int64_t lda, int* piv,
 
 // The tensor-core factorization in slabs of two 128-column panels: the
 // trailing matrix is updated once per slab (K = 256), which halves its reads
-// and writes, the bound of that update.  Per slab [s0, s1):
-//   panel A = columns [s0, s0 + 128): factor, interchanges on the other columns;
-//   the slab's other half: its rows of U (trsm with A's L11), the rows below
-//     updated with K = 128, then panel B factored and its interchanges applied;
-//   the trailing columns: rows of U by two trsm steps with the update between
-//     them (the 256 x 256 unit lower L11 of the slab), then one update of the
-//     trailing block with K = 256 on the tensor cores.
-// The two K = 128 updates inside a slab (128 columns, or 128 rows) run as
-// FP32 CUDA-core GEMMs: one launch each, at least as accurate as any of the
-// tensor-core operand formats.
-static int getrf_tc_slabs(luhot_ctx* ctx, int m, int n, float* a, int64_t lda, int* piv, int tc_kind, void* tc_a,
-                          void* tc_b, float* tc_scal, cudaStream_t stream) {
+// and writes, the bound of that update.  The two K = 128 updates inside a
+// slab (128 columns, or 128 rows) run as FP32 CUDA-core GEMMs: one launch
+// each, at least as accurate as any of the tensor-core operand formats.
+//
+// Look-ahead: the trailing update of slab s is cut at the next slab's
+// columns.  A high-priority stream (hs) factors slab s (panels A and B,
+// their interchanges on the slab's own columns, the K = 128 step between
+// them), then brings the next slab's columns up to date (interchanges, rows
+// of U, update).  A low-priority stream (ls) then does the rest of slab s:
+// its interchanges on the columns left of it and right of the next slab,
+// the rows of U there and the update of those columns, on at most SM count
+// - 64 CTAs, so that slab s + 1's panels (64 CTAs) run beside it.  hs waits
+// for the rest of slab s - 2 before slab s's panels (it covered slab s's
+// columns) and for the rest of slab s - 1 before the next slab's columns.
+// Each panel's list of moved rows is saved per slab parity for ls.
+static int* la_saved_moves(luhot_ctx* ctx, int parity, int half) {
+  return reinterpret_cast<int*>(static_cast<char*>(ctx->la_moves.ptr) + (size_t)(2 * parity + half) * kPanelMovesBytes);
+}
+
+// Launches between its construction and destruction go to `s` (the
+// profile's events are recorded on the context's stream).
+struct OnStream {
+  luhot_ctx* ctx;
+  cudaStream_t old;
+  OnStream(luhot_ctx* c, cudaStream_t s) : ctx(c), old(c->stream) { c->stream = s; }
+  ~OnStream() { ctx->stream = old; }
+};
+
+static int la_setup(luhot_ctx* ctx) {
+  if (!ctx->la_hi) {
+    int least = 0, greatest = 0;
+    LUHOT_CUDA_TRY(ctx, cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    LUHOT_CUDA_TRY(ctx, cudaStreamCreateWithPriority(&ctx->la_lo, cudaStreamNonBlocking, least));
+    LUHOT_CUDA_TRY(ctx, cudaStreamCreateWithPriority(&ctx->la_hi, cudaStreamNonBlocking, greatest));
+  }
+  for (auto& e : ctx->la_ev)
+    if (!e) LUHOT_CUDA_TRY(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  return ensure_buf(ctx, ctx->la_moves, 4 * kPanelMovesBytes);
+}
+
+// Rows [s0, s1) of U on the columns [c0, c1) (two trsm steps with the K =
+// 128 update of panel B's rows between them), then the update of rows
+// [s1, m) x columns [c0, c1) on the tensor cores (K = s1 - s0).
+static int slab_columns(luhot_ctx* ctx, float* a, int64_t lda, int m, int s0, int h0, int h1, int c0, int c1,
+                        int tc_kind, void* tc_a, void* tc_b, float* tc_scal, cudaStream_t st) {
+  if (c0 >= c1) return LUHOT_OK;
+  int rc = launch_trsm<float, false>(ctx, a, lda, s0, h0, c0, c1, st);
+  if (!rc && h1 > 0) {
+    rc = launch_gemm<float, false>(ctx, a, lda, s0 + h0, c0, s0, h0, h1, c1 - c0, st);
+    if (!rc) rc = launch_trsm<float, false>(ctx, a, lda, s0 + h0, h1, c0, c1, st);
+  }
+  const int s1 = s0 + h0 + h1;
+  if (!rc) rc = tc_gemm_update(ctx, tc_kind, a, lda, s0, h0 + h1, s1, m, c0, c1, tc_a, tc_b, tc_scal, st);
+  return rc;
+}
+
+static int tc_slab_loop(luhot_ctx* ctx, int m, int n, float* a, int64_t lda, int* piv, int tc_kind, void* tc_a,
+                        void* tc_b, float* tc_scal) {
   const int dim_min = std::min(m, n);
-  LUHOT_CUDA_TRY(ctx, cudaMemsetAsync(ctx->panel_scratch, 0, kPanelScratchBytes, stream));
-  constexpr int hw = kTcPanelWidth;
-  for (int s0 = 0; s0 < dim_min; s0 += 2 * hw) {
-    const int sw = std::min(2 * hw, dim_min - s0);
+  cudaStream_t hs = ctx->la_hi, ls = ctx->la_lo;
+  cudaEvent_t ev_ready = ctx->la_ev[1];
+  const int* live_moves = reinterpret_cast<const int*>(static_cast<char*>(ctx->panel_scratch) + kPanelSlotBytes);
+  constexpr int hw = kTcPanelWidth, sl = 2 * hw;
+  const int cap_rest = std::max(1, ctx->num_sms - 64);
+  int slab = 0;
+  for (int s0 = 0; s0 < dim_min; s0 += sl, ++slab) {
+    const int sw = std::min(sl, dim_min - s0);
     const int h0 = std::min(hw, sw), h1 = sw - h0;
     const int s1 = s0 + sw;
-    int rc = launch_panel<float, false>(ctx, a, lda, m, s0, h0, piv, stream);
-    if (!rc) rc = launch_laswp<float>(ctx, a, lda, s0, h0, n, stream);
-    if (!rc && h1 > 0) {
-      rc = launch_trsm<float, false>(ctx, a, lda, s0, h0, s0 + h0, s1, stream);
-      if (!rc) rc = launch_gemm<float, false>(ctx, a, lda, s0 + h0, s0 + h0, s0, h0, m - (s0 + h0), h1, stream);
-      if (!rc) rc = launch_panel<float, false>(ctx, a, lda, m, s0 + h0, h1, piv, stream);
-      if (!rc) rc = launch_laswp<float>(ctx, a, lda, s0 + h0, h1, n, stream);
-    }
-    if (!rc && s1 < n) {
-      rc = launch_trsm<float, false>(ctx, a, lda, s0, h0, s1, n, stream);
+    const int e1 = std::min(n, s1 + sl);  // the next slab's columns: [s1, e1)
+    const int par = slab & 1;
+    int* mv_a = la_saved_moves(ctx, par, 0);
+    int* mv_b = la_saved_moves(ctx, par, 1);
+    {
+      OnStream on(ctx, hs);
+      if (slab >= 2) LUHOT_CUDA_TRY(ctx, cudaStreamWaitEvent(hs, ctx->la_ev[2 + par], 0));
+      int rc = launch_panel<float, false>(ctx, a, lda, m, s0, h0, piv, hs);
+      if (rc) return rc;
+      LUHOT_CUDA_TRY(ctx, cudaMemcpyAsync(mv_a, live_moves, kPanelMovesBytes, cudaMemcpyDeviceToDevice, hs));
+      rc = launch_laswp_cols<float>(ctx, a, lda, mv_a, h0, 0, 0, s0 + h0, s1, hs);
       if (!rc && h1 > 0) {
-        rc = launch_gemm<float, false>(ctx, a, lda, s0 + h0, s1, s0, h0, h1, n - s1, stream);
-        if (!rc) rc = launch_trsm<float, false>(ctx, a, lda, s0 + h0, h1, s1, n, stream);
+        rc = launch_trsm<float, false>(ctx, a, lda, s0, h0, s0 + h0, s1, hs);
+        if (!rc) rc = launch_gemm<float, false>(ctx, a, lda, s0 + h0, s0 + h0, s0, h0, m - (s0 + h0), h1, hs);
+        if (!rc) rc = launch_panel<float, false>(ctx, a, lda, m, s0 + h0, h1, piv, hs);
+        if (rc) return rc;
+        LUHOT_CUDA_TRY(ctx, cudaMemcpyAsync(mv_b, live_moves, kPanelMovesBytes, cudaMemcpyDeviceToDevice, hs));
+        rc = launch_laswp_cols<float>(ctx, a, lda, mv_b, h1, s0, s0 + h0, 0, 0, hs);
       }
-      if (!rc) rc = tc_gemm_update(ctx, tc_kind, a, lda, s0, sw, s1, m, s1, n, tc_a, tc_b, tc_scal, stream);
+      if (!rc && s1 < e1) {
+        if (slab >= 1) LUHOT_CUDA_TRY(ctx, cudaStreamWaitEvent(hs, ctx->la_ev[2 + (par ^ 1)], 0));
+        rc = launch_laswp_cols<float>(ctx, a, lda, mv_a, h0, 0, 0, s1, e1, hs);
+        if (!rc && h1 > 0) rc = launch_laswp_cols<float>(ctx, a, lda, mv_b, h1, 0, 0, s1, e1, hs);
+        if (!rc) rc = slab_columns(ctx, a, lda, m, s0, h0, h1, s1, e1, tc_kind, tc_a, tc_b, tc_scal, hs);
+      }
+      if (rc) return rc;
+      LUHOT_CUDA_TRY(ctx, cudaEventRecord(ev_ready, hs));
     }
-    if (rc) return rc;
+    {
+      OnStream on(ctx, ls);
+      LUHOT_CUDA_TRY(ctx, cudaStreamWaitEvent(ls, ev_ready, 0));
+      int rc = launch_laswp_cols<float>(ctx, a, lda, mv_a, h0, 0, s0, e1, n, ls);
+      if (!rc && h1 > 0) rc = launch_laswp_cols<float>(ctx, a, lda, mv_b, h1, 0, s0, e1, n, ls);
+      if (!rc && e1 < n) {
+        ctx->tc_grid_cap = cap_rest;
+        rc = slab_columns(ctx, a, lda, m, s0, h0, h1, e1, n, tc_kind, tc_a, tc_b, tc_scal, ls);
+        ctx->tc_grid_cap = 0;
+      }
+      if (rc) return rc;
+      LUHOT_CUDA_TRY(ctx, cudaEventRecord(ctx->la_ev[2 + par], ls));
+    }
   }
+  return LUHOT_OK;
+}
+
+static int getrf_tc_slabs(luhot_ctx* ctx, int m, int n, float* a, int64_t lda, int* piv, int tc_kind, void* tc_a,
+                          void* tc_b, float* tc_scal, cudaStream_t stream) {
+  LUHOT_CUDA_TRY(ctx, cudaMemsetAsync(ctx->panel_scratch, 0, kPanelScratchBytes, stream));
+  int rc = la_setup(ctx);
+  if (rc) return rc;
+  LUHOT_CUDA_TRY(ctx, cudaEventRecord(ctx->la_ev[0], stream));
+  LUHOT_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->la_hi, ctx->la_ev[0], 0));
+  LUHOT_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->la_lo, ctx->la_ev[0], 0));
+  rc = tc_slab_loop(ctx, m, n, a, lda, piv, tc_kind, tc_a, tc_b, tc_scal);
+  ctx->tc_grid_cap = 0;
+  // The caller's stream waits for both streams, also after an error.
+  cudaError_t e = cudaEventRecord(ctx->la_ev[0], ctx->la_hi);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(stream, ctx->la_ev[0], 0);
+  if (e == cudaSuccess) e = cudaEventRecord(ctx->la_ev[1], ctx->la_lo);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(stream, ctx->la_ev[1], 0);
+  if (rc) return rc;
+  if (e != cudaSuccess) return set_error(ctx, LUHOT_ERR_CUDA, std::string("look-ahead join: ") + cudaGetErrorString(e));
   return LUHOT_OK;
 }
 

@@ -86,6 +86,14 @@ struct luhot_ctx {
   luhot::DevBuf chain_buf;                  // chained sweeps: tagged x words + ticket
   luhot::DevBuf scaled_buf;                 // GMRES-IR: block-scaled tiles of the FP32 factor
   luhot::DevBuf oz_buf;                     // FP64 getrf: digit slices of the tensor-core update
+  // Look-ahead of the tensor-core LU: a high-priority stream for the panels
+  // and the next slab's columns, a low-priority one for the rest of each
+  // trailing update, their events (start, ready, rest of even / odd slabs)
+  // and the saved move lists of the panels (two slabs x two panels).
+  cudaStream_t la_hi = nullptr, la_lo = nullptr;
+  cudaEvent_t la_ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  luhot::DevBuf la_moves;
+  int tc_grid_cap = 0;  // CTAs of the persistent tensor-core update at most (0: one per SM)
   unsigned int chain_epoch = 0;             // tag of the last chained sweep (0 = none)
   double* h_scalars = nullptr;              // pinned: scalars read back by the refinement loop
   void* h_piv = nullptr;                    // pinned pivots staging

@@ -784,9 +784,10 @@ static int launch_tc(luhot_ctx* ctx, float* a, int64_t lda, int k0, int w, int r
     auto kern = tc_gemm_persistent_kernel<KIND>;
     LUHOT_CUDA_TRY(ctx, allow_max_dynamic_smem(kern));
     const int tiles = ((M + 127) / 128) * ((N + 127) / 128);
+    const int cap = ctx->tc_grid_cap > 0 ? std::min(ctx->tc_grid_cap, ctx->num_sms) : ctx->num_sms;
     prof_begin(ctx, kProfGemm);
-    kern<<<std::min(tiles, ctx->num_sms), kTcThreads, TcShape<KIND>::kSmem, stream>>>(tA, tB, tC, M, N, kalloc,
-                                                                                    scal + 4, ctx->d_status);
+    kern<<<std::min(tiles, cap), kTcThreads, TcShape<KIND>::kSmem, stream>>>(tA, tB, tC, M, N, kalloc, scal + 4,
+                                                                           ctx->d_status);
   } else {
     const int kbox = KIND == kTcTF32 ? 32 : 64;
     const size_t smem = KIND == kTcBF16x3 ? 1024 + 6 * 16384 : 1024 + (size_t)(kalloc / kbox) * 2 * 16384;
