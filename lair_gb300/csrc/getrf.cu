@@ -738,44 +738,57 @@ __global__ void __launch_bounds__(kTrsmCols) trsm_kernel(T* a, int64_t lda, int 
 // broadcast from shared memory with L11 stored transposed), then solves the
 // 16 x 16 diagonal block.  x lives in shared memory (one column per thread,
 // conflict-free).  W = 64 or 128 >= w; L11 is zero-padded to W x W.  The
-// exact mode keeps trsm_kernel's order.
+// CTA's 256 threads stage L11 and the 64 columns of A12 together (the
+// loads, not the solve, were most of the time with 64 threads); the first
+// 64 then solve and all of them write the rows back.  The exact mode keeps
+// trsm_kernel's order.
+constexpr int kTrsmFastThreads = 256;
+
 template <typename T, int W>
-__global__ void __launch_bounds__(kTrsmCols) trsm_fast_kernel(T* a, int64_t lda, int k0, int w, int c0, int n) {
+__global__ void __launch_bounds__(kTrsmFastThreads) trsm_fast_kernel(T* a, int64_t lda, int k0, int w, int c0,
+                                                                      int n) {
   constexpr int RB = 16;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* Lt = reinterpret_cast<T*>(smem_raw);  // [W][W]: Lt[k][i] = L11[i][k] for i > k, else 0
   T* X = Lt + W * W;                       // [W][kTrsmCols]
   const int tid = threadIdx.x;
+  const int cb = c0 + blockIdx.x * kTrsmCols;
   for (int idx = tid; idx < W * W; idx += blockDim.x) {
     const int k = idx / W, i = idx - k * W;
     Lt[idx] = (i > k && i < w && k < w) ? a[(int64_t)(k0 + i) * lda + k0 + k] : T(0);
   }
-  const int c = c0 + blockIdx.x * kTrsmCols + tid;
-  const bool active = c < n;
-  for (int i = 0; i < W; ++i) X[i * kTrsmCols + tid] = (active && i < w) ? a[(int64_t)(k0 + i) * lda + c] : T(0);
-  __syncthreads();
-  for (int i0 = 0; i0 < w; i0 += RB) {
-    T acc[RB];
-#pragma unroll
-    for (int r = 0; r < RB; ++r) acc[r] = X[(i0 + r) * kTrsmCols + tid];
-    for (int k = 0; k < i0; ++k) {
-      const T xk = X[k * kTrsmCols + tid];
-      const T* lk = Lt + k * W + i0;
-#pragma unroll
-      for (int r = 0; r < RB; ++r) acc[r] = fma(-lk[r], xk, acc[r]);
-    }
-#pragma unroll
-    for (int kk = 0; kk < RB - 1; ++kk) {
-      const T* lk = Lt + (i0 + kk) * W + i0;
-#pragma unroll
-      for (int r = 0; r < RB; ++r)
-        if (r > kk) acc[r] = fma(-lk[r], acc[kk], acc[r]);
-    }
-#pragma unroll
-    for (int r = 0; r < RB; ++r) X[(i0 + r) * kTrsmCols + tid] = acc[r];
+  for (int idx = tid; idx < W * kTrsmCols; idx += blockDim.x) {
+    const int i = idx / kTrsmCols, cc = idx - i * kTrsmCols;
+    X[idx] = (cb + cc < n && i < w) ? a[(int64_t)(k0 + i) * lda + cb + cc] : T(0);
   }
-  if (active)
-    for (int i = 1; i < w; ++i) a[(int64_t)(k0 + i) * lda + c] = X[i * kTrsmCols + tid];
+  __syncthreads();
+  if (tid < kTrsmCols) {
+    for (int i0 = 0; i0 < w; i0 += RB) {
+      T acc[RB];
+#pragma unroll
+      for (int r = 0; r < RB; ++r) acc[r] = X[(i0 + r) * kTrsmCols + tid];
+      for (int k = 0; k < i0; ++k) {
+        const T xk = X[k * kTrsmCols + tid];
+        const T* lk = Lt + k * W + i0;
+#pragma unroll
+        for (int r = 0; r < RB; ++r) acc[r] = fma(-lk[r], xk, acc[r]);
+      }
+#pragma unroll
+      for (int kk = 0; kk < RB - 1; ++kk) {
+        const T* lk = Lt + (i0 + kk) * W + i0;
+#pragma unroll
+        for (int r = 0; r < RB; ++r)
+          if (r > kk) acc[r] = fma(-lk[r], acc[kk], acc[r]);
+      }
+#pragma unroll
+      for (int r = 0; r < RB; ++r) X[(i0 + r) * kTrsmCols + tid] = acc[r];
+    }
+  }
+  __syncthreads();
+  for (int idx = kTrsmCols + tid; idx < w * kTrsmCols; idx += blockDim.x) {
+    const int i = idx / kTrsmCols, cc = idx - i * kTrsmCols;
+    if (cb + cc < n) a[(int64_t)(k0 + i) * lda + cb + cc] = X[idx];
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1213,12 +1226,12 @@ static int launch_trsm(luhot_ctx* ctx, T* a, int64_t lda, int k0, int w, int c_b
   if (!kExact && w <= 64) {
     const size_t smem = ((size_t)64 * 64 + (size_t)64 * kTrsmCols) * sizeof(T);
     LUHOT_CUDA_TRY(ctx, allow_max_dynamic_smem(trsm_fast_kernel<T, 64>));
-    trsm_fast_kernel<T, 64><<<tgrid, kTrsmCols, smem, stream>>>(a, lda, k0, w, c_begin, c_end);
+    trsm_fast_kernel<T, 64><<<tgrid, kTrsmFastThreads, smem, stream>>>(a, lda, k0, w, c_begin, c_end);
   } else if (!kExact && std::is_same<T, float>::value && w <= 128) {
     if constexpr (std::is_same<T, float>::value) {
       const size_t smem = ((size_t)128 * 128 + (size_t)128 * kTrsmCols) * sizeof(T);
       LUHOT_CUDA_TRY(ctx, allow_max_dynamic_smem(trsm_fast_kernel<T, 128>));
-      trsm_fast_kernel<T, 128><<<tgrid, kTrsmCols, smem, stream>>>(a, lda, k0, w, c_begin, c_end);
+      trsm_fast_kernel<T, 128><<<tgrid, kTrsmFastThreads, smem, stream>>>(a, lda, k0, w, c_begin, c_end);
     }
   } else {
     const size_t smem = ((size_t)w * w + (size_t)w * kTrsmCols) * sizeof(T);

@@ -80,3 +80,36 @@ def test_gmres_ir_with_11_bit_factors_converges_at_kappa_1e4(kind):
     assert rc == _lib.LUHOT_OK and info.converged
     assert berr <= n * 2.0 ** -53
     assert info.inner_iterations <= 2 * inner_e + 10
+
+
+@pytest.mark.parametrize("kind", ["bf16x3", "tf32"])
+@pytest.mark.parametrize("m,n", [(1000, 1000), (1300, 700), (700, 1300), (257, 257), (129, 900), (900, 129)])
+def test_tensor_core_factor_shapes(kind, m, n):
+    """The tensor-core factorization runs in slabs of 256 columns with a
+    look-ahead (the next slab's columns on one stream, the rest of each
+    trailing update on another).  On square, tall and wide shapes whose sizes
+    are not multiples of the slab, the factor reproduces P A = L U to the
+    accuracy of its operand format: max |PA - LU| / max |A| at most 64 n 2^-24
+    for the FP32-accurate BF16x3 products and 16 sqrt(n) 2^-11 for TF32 (a
+    missed or repeated update would leave O(1) entries)."""
+    torch = pytest.importorskip("torch")
+    lib, ctx = _lib.load(), _lib.context()
+    a = np.random.default_rng(m * 7 + n).standard_normal((m, n)).astype(np.float32)
+    d = torch.from_numpy(a).cuda()
+    k = min(m, n)
+    piv = torch.zeros(k, dtype=torch.int32, device="cuda")
+    sing = ctypes.c_int64(0)
+    torch.cuda.synchronize()
+    _lib.check(lib.luhot_sgetrf_mixed_dev(ctx, m, n, d.data_ptr(), n, piv.data_ptr(), _lib.PRECISIONS[kind],
+                                          ctypes.byref(sing)), ctx)
+    assert sing.value == -1
+    lu = d.cpu().numpy().astype(np.float64)
+    lo = np.tril(lu, -1)[:, :k] + np.eye(m, k)
+    up = np.triu(lu)[:k, :]
+    pa = a.astype(np.float64)
+    for i, p in enumerate(piv.cpu().numpy()):
+        pa[[i, p]] = pa[[p, i]]
+    bound = 64 * max(m, n) * 2.0 ** -24 if kind == "bf16x3" else 16 * np.sqrt(max(m, n)) * 2.0 ** -11
+    err = np.abs(pa - lo @ up).max() / np.abs(a).max()
+    assert err <= bound, err
+    assert np.abs(np.tril(lu, -1)).max() <= 1.0 + 1e-6  # partial pivoting: |L| <= 1
