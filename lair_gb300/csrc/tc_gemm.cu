@@ -301,7 +301,11 @@ __global__ void __launch_bounds__(128) tc_gemm_x3_kernel(const __grid_constant__
 //   warp 0      TMA producer: per tile and 128-byte K box, the A and B boxes
 //               (three pieces each for kTcBF16x3) into a ring of stages;
 //   warp 1      TMEM owner and MMA issuer: two 128-column FP32 accumulators,
-//               so one tile's MMAs overlap the previous tile's epilogue;
+//               so one tile's MMAs overlap the previous tile's epilogue
+//               (BF16x3: two pairs, the leading product a0 b0 in one, the
+//               five smaller products in the other, added in the epilogue:
+//               the tensor core's accumulation then never rounds the small
+//               terms against the large running sum);
 //   warps 2-5   epilogue: tcgen05.ld of their 32 TMEM lanes, scale by alpha,
 //               stage 128 x 32 FP32 blocks in shared memory (128-byte
 //               swizzle) and add them into C with TMA reduce-add, so C is
@@ -326,6 +330,19 @@ struct TcShape {
   static constexpr int kStagingBytes = 2 * 16384;
   static constexpr size_t kSmem = 1024 + (size_t)kStages * kStageBytes + kStagingBytes;
 };
+
+// 32 consecutive 32-bit TMEM columns of the warp's 32 lanes (completed by
+// tcgen05.wait::ld).
+__device__ __forceinline__ void tc_ld32(unsigned taddr, unsigned (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,"
+      "%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+}
 
 __device__ __forceinline__ void tc_abort(DeviceStatus* st, int* s_abort) {
   atomicCAS(&st->error, kDevOk, kDevBarrierTimeout);
@@ -358,8 +375,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const int t_end = (int)((int64_t)(blockIdx.x + 1) * tiles / G);
   const int nkb = kalloc / Sh::kKBox;
 
+  // BF16x3 keeps the leading product a0 b0 and the five smaller ones in
+  // separate accumulators (added once, in the epilogue), so the small terms
+  // are not rounded against the large running sum at every k-step.
+  constexpr bool kSplitAcc = KIND == kTcBF16x3;
+  constexpr unsigned kAccCols = kSplitAcc ? 256u : 128u;  // TMEM columns per accumulator buffer
   if (warp == 1) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(smem_u32(&tmem_base)));
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                 "n"(2 * kAccCols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   if (threadIdx.x == 0) {
@@ -432,7 +455,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;");
-        const unsigned acc_addr = tmem + (unsigned)(b * 128);
+        const unsigned acc_addr = tmem + (unsigned)b * kAccCols;
         bool ok = true;
         for (int kb = 0; kb < nkb; ++kb, ++it) {
           const int s = it % S;
@@ -448,16 +471,18 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             for (int pr = 0; pr < NPROD; ++pr) {
               const unsigned long long da = sw128_desc(smem_u32(sa + pa[pr] * 16384 + ks * 32));
               const unsigned long long db = sw128_desc(smem_u32(sb + pb[pr] * 16384 + ks * 32));
-              const unsigned accf = (kb > 0 || ks > 0 || pr > 0) ? 1u : 0u;
+              const bool lo = kSplitAcc && pr > 0;
+              const unsigned accf = (kb > 0 || ks > 0 || pr > (lo ? 1 : 0)) ? 1u : 0u;
+              const unsigned acc = acc_addr + (lo ? 128u : 0u);
               if (KIND == kTcTF32)
                 asm volatile(
                     "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, "
-                    "p;\n}\n" ::"r"(acc_addr),
+                    "p;\n}\n" ::"r"(acc),
                     "l"(da), "l"(db), "r"(idesc), "r"(accf));
               else
                 asm volatile(
                     "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, "
-                    "p;\n}\n" ::"r"(acc_addr),
+                    "p;\n}\n" ::"r"(acc),
                     "l"(da), "l"(db), "r"(idesc), "r"(accf));
             }
           }
@@ -499,16 +524,17 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       asm volatile("tcgen05.fence::after_thread_sync;");
       for (int cb = 0; cb < 4; ++cb, sbuf ^= 1) {
         unsigned r[32];
-        const unsigned taddr = tmem + ((unsigned)(quarter * 32) << 16) + (unsigned)(b * 128 + cb * 32);
-        asm volatile(
-            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,"
-            "%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-              "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-              "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-            : "r"(taddr));
-        asm volatile("tcgen05.wait::ld.sync.aligned;");
+        const unsigned taddr = tmem + ((unsigned)(quarter * 32) << 16) + (unsigned)b * kAccCols + (unsigned)(cb * 32);
+        tc_ld32(taddr, r);
+        if constexpr (kSplitAcc) {
+          unsigned r2[32];
+          tc_ld32(taddr + 128u, r2);
+          asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+          for (int q = 0; q < 32; ++q) r[q] = __float_as_uint(__uint_as_float(r[q]) + __uint_as_float(r2[q]));
+        } else {
+          asm volatile("tcgen05.wait::ld.sync.aligned;");
+        }
         if (cb == 3) {
           // This warp is done with the accumulator: the MMA warp may reuse it.
           asm volatile("tcgen05.fence::before_thread_sync;");
@@ -561,7 +587,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
-  if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem));
+  if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(2 * kAccCols));
 }
 
 // ---------------------------------------------------------------------------
