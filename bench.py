@@ -399,6 +399,38 @@ def run_ours(args):
     ms_max = float(t.item())
     value = world * args.steps * flops_of(n, nrhs) / (ms_max * 1e-3) / 1e9
 
+    # e2e: equation::solve through the C ABI with host buffers every step, right
+    # after the device-resident steps (same GPU state as the timed region)
+    e2e = None
+    if not args.no_e2e:
+        A_h = A0.cpu().numpy()
+        B_h = B0.cpu().numpy()
+        X_h = np.empty_like(B_h)
+        _lib.check(lib.luhot_set_stream(ctx, None), ctx)
+
+        def e2e_step():
+            rc = lib.luhot_dgesv(ctx, n, nrhs, A_h.ctypes.data, n, 1, B_h.ctypes.data, nrhs, 1,
+                                 X_h.ctypes.data, nrhs, 1, mode)
+            _lib.check(rc, ctx)
+
+        for _ in range(max(1, min(args.warmup, 2))):
+            e2e_step()
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        barrier()
+        dt = time.perf_counter() - t0
+        tt = torch.tensor([dt], dtype=torch.float64, device="cuda")
+        if world > 1:
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        dt = float(tt.item())
+        e2e = {"value": world * args.steps * flops_of(n, nrhs) / dt / 1e9, "unit": "GFLOP/s",
+               "h2d_bytes_per_step": int(A_h.nbytes + B_h.nbytes), "d2h_bytes_per_step": int(X_h.nbytes),
+               "api": "luhot_dgesv (host A, B in; host X out; pageable numpy buffers, page-locked by the call)",
+               "ms_per_step": dt / args.steps * 1e3}
+        _lib.check(lib.luhot_set_stream(ctx, ctypes.c_void_p(stream.cuda_stream)), ctx)
+
     # backward error of the last solve (FP64 on the GPU)
     R = B0 - A0 @ X
     berr = (R.abs().max() / (A0.abs().sum(1).max() * X.abs().max() + B0.abs().max())).item()
@@ -469,37 +501,6 @@ def run_ours(args):
     resident = None
     if not args.no_resident:
         resident = run_resident_solve(args, lib, ctx, torch, A0, A, piv, peak)
-
-    # e2e: equation::solve through the C ABI with host buffers every step
-    e2e = None
-    if not args.no_e2e:
-        A_h = A0.cpu().numpy()
-        B_h = B0.cpu().numpy()
-        X_h = np.empty_like(B_h)
-        _lib.check(lib.luhot_set_stream(ctx, None), ctx)
-
-        def e2e_step():
-            rc = lib.luhot_dgesv(ctx, n, nrhs, A_h.ctypes.data, n, 1, B_h.ctypes.data, nrhs, 1,
-                                 X_h.ctypes.data, nrhs, 1, mode)
-            _lib.check(rc, ctx)
-
-        for _ in range(max(1, min(args.warmup, 2))):
-            e2e_step()
-        barrier()
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
-            e2e_step()
-        barrier()
-        dt = time.perf_counter() - t0
-        tt = torch.tensor([dt], dtype=torch.float64, device="cuda")
-        if world > 1:
-            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        dt = float(tt.item())
-        e2e = {"value": world * args.steps * flops_of(n, nrhs) / dt / 1e9, "unit": "GFLOP/s",
-               "h2d_bytes_per_step": int(A_h.nbytes + B_h.nbytes), "d2h_bytes_per_step": int(X_h.nbytes),
-               "api": "luhot_dgesv (host A, B in; host X out; pageable numpy buffers, page-locked by the call)",
-               "ms_per_step": dt / args.steps * 1e3}
-        _lib.check(lib.luhot_set_stream(ctx, ctypes.c_void_p(stream.cuda_stream)), ctx)
 
     ir = None
     if not args.no_ir:
