@@ -76,9 +76,12 @@ int luhot_set_block(luhot_ctx* ctx, int nb);
  * updated on the FP16 tensor cores by an exact integer-slice product (Ozaki
  * scheme: seven 8-bit slices per operand, 28 slice products, FP32 sums that
  * are exact, one FP64 rounding; error at or below an FP64 GEMM's), smaller
- * ones on the FP64 tensor cores (DMMA).  LUHOT_UPDATE_DMMA: DMMA only.
+ * ones on the FP64 tensor cores (DMMA); the U12 solves of at least 256
+ * columns run as the same product, U12 = A12 - (I - L11^-1) A12.
+ * LUHOT_UPDATE_DMMA: DMMA updates and FMA substitutions only.
  * LUHOT_UPDATE_OZAKI: the tensor-core product on every block of at least
- * 128 x 64.  Exact mode and FP32 ignore the setting. */
+ * 128 x 64 (U12 solves from 128 columns).  Exact mode and FP32 ignore the
+ * setting. */
 #define LUHOT_UPDATE_AUTO 0
 #define LUHOT_UPDATE_DMMA 1
 #define LUHOT_UPDATE_OZAKI 2
