@@ -130,11 +130,52 @@ __global__ void copy_rows_kernel(unsigned char* dst, size_t dpitch, const unsign
   }
 }
 
+// Host -> device copy by 16-byte SM loads from pageable host memory that the
+// GPU reaches through the host's page tables: no page-locking, and on GB300
+// over C2C as fast as the copy engines from locked memory (206 against 189
+// GB/s measured for 2 GiB).
+__global__ void copy_from_host_kernel(const uint4* __restrict__ src, uint4* __restrict__ dst, size_t n16) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += (size_t)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+}
+
+// A host array of at least this many bytes is copied in by SM loads (on
+// hosts whose GPU reads pageable memory) or page-locked for the call.
+constexpr size_t kLargeHostBytes = (size_t)8 << 20;
+
+static bool host_direct_source(luhot_ctx* ctx, const void* src, size_t bytes) {
+  if (!ctx->host_direct || bytes < kLargeHostBytes || bytes % 16 != 0 ||
+      (reinterpret_cast<uintptr_t>(src) & 15) != 0)
+    return false;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, src) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeUnregistered;
+}
+
+// A host input (m x n, element strides) that stage_in will copy as one
+// contiguous block into a device matrix of leading dimension ldd by SM loads.
+static bool direct_input(luhot_ctx* ctx, int64_t m, int64_t n, int64_t rs, int64_t cs, int64_t ldd, size_t elem) {
+  if (!ctx->host_direct || m <= 0 || n <= 0 || cs != 1 || (m > 1 && rs != n) || ldd != n) return false;
+  return (size_t)(m * n) * elem >= kLargeHostBytes;
+}
+
 int copy_2d(luhot_ctx* ctx, void* dst, size_t dpitch, const void* src, size_t spitch, size_t wbytes, size_t rows,
             cudaMemcpyKind kind) {
   if (wbytes == 0 || rows == 0) return LUHOT_OK;
   if ((dpitch == wbytes && spitch == wbytes) || rows == 1) {
-    LUHOT_CUDA_TRY(ctx, cudaMemcpyAsync(dst, src, wbytes * rows, kind, ctx->stream));
+    const size_t bytes = wbytes * rows;
+    if (kind == cudaMemcpyHostToDevice && (reinterpret_cast<uintptr_t>(dst) & 15) == 0 &&
+        host_direct_source(ctx, src, bytes)) {
+      copy_from_host_kernel<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(static_cast<const uint4*>(src),
+                                                                     static_cast<uint4*>(dst), bytes / 16);
+      count_launch(ctx);
+      LUHOT_CUDA_TRY(ctx, cudaGetLastError());
+      return LUHOT_OK;
+    }
+    LUHOT_CUDA_TRY(ctx, cudaMemcpyAsync(dst, src, bytes, kind, ctx->stream));
     return LUHOT_OK;
   }
   if (kind == cudaMemcpyDeviceToDevice && wbytes % 4 == 0 && dpitch % 4 == 0 && spitch % 4 == 0 &&
@@ -283,7 +324,7 @@ HostPin::HostPin(luhot_ctx* c, const void* base, int64_t m, int64_t n, int64_t r
     : ctx(c) {
   if (!base || m <= 0 || n <= 0 || rs < 0 || cs < 0) return;
   const size_t span = ((size_t)(m - 1) * (size_t)rs + (size_t)(n - 1) * (size_t)cs + 1) * elem;
-  if (span < (size_t)8 << 20) return;
+  if (span < kLargeHostBytes) return;
   const uintptr_t lo = reinterpret_cast<uintptr_t>(base), hi = lo + span;
   std::lock_guard<std::mutex> lock(g_pin_mu);
   // A call on another context may have pinned this array (or part of it):
@@ -472,6 +513,13 @@ int luhot_create(luhot_ctx** out, int device) {
   }
   cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
   cudaDeviceGetAttribute(&ctx->max_smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+  {
+    int pageable = 0, host_tables = 0;
+    cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device);
+    cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device);
+    ctx->host_direct = pageable == 1 && host_tables == 1;
+    cudaGetLastError();
+  }
   bool ok = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) == cudaSuccess;
   ctx->stream = ctx->own_stream;
   ok = ok && cudaMalloc(&ctx->d_status, sizeof(DeviceStatus)) == cudaSuccess;
@@ -616,8 +664,11 @@ int luhot_dgesv(luhot_ctx* ctx, int64_t n, int64_t nrhs, const double* a, int64_
   if (n == 0 || nrhs == 0) return LUHOT_OK;
   if (!a || !b || !x) return set_error(ctx, LUHOT_ERR_INVALID_ARG, "gesv: null pointer");
   const int64_t lda = dev_ld<double>(n);
-  HostPin pin_a(ctx, a, n, n, rs, cs, sizeof(double));
-  HostPin pin_b(ctx, b, n, nrhs, b_rs, b_cs, sizeof(double));
+  // A and B are only read: on hosts whose GPU reads pageable memory their
+  // contiguous row-major copies go by SM loads (copy_2d) with no page-locking.
+  HostPin pin_a(ctx, direct_input(ctx, n, n, rs, cs, lda, sizeof(double)) ? nullptr : a, n, n, rs, cs, sizeof(double));
+  HostPin pin_b(ctx, direct_input(ctx, n, nrhs, b_rs, b_cs, nrhs, sizeof(double)) ? nullptr : b, n, nrhs, b_rs, b_cs,
+                sizeof(double));
   HostPin pin_x(ctx, x, n, nrhs, x_rs, x_cs, sizeof(double));
   int rc = ensure_buf(ctx, ctx->work[0], (size_t)n * lda * sizeof(double));
   if (rc) return rc;

@@ -100,6 +100,10 @@ struct luhot_ctx {
   size_t h_piv_bytes = 0;
   int nb_override = 0;
   int fp64_update = LUHOT_UPDATE_AUTO;  // Schur-update engine of fast-mode FP64 getrf
+  // The GPU reads pageable host memory through the host's page tables
+  // (Grace: address translation services), so large host inputs are copied
+  // by SM loads instead of being page-locked for the copy engines.
+  bool host_direct = false;
   bool trace = false;  // LUHOT_TRACE=1: refinement steps are reported on stderr
   unsigned long long wait_timeout_ns = 2000000000ull;  // per device-side wait
   std::atomic<int64_t> launches{0};
