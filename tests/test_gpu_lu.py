@@ -277,6 +277,28 @@ def test_gesv_matches_factor_then_solve():
     np.testing.assert_array_equal(x, lapack.getrs(a, piv, b))
 
 
+@pytest.mark.parametrize("n,order", [(1024, "C"), (1536, "C"), (1024, "F")])
+def test_gesv_large_host_inputs(n, order):
+    """Host inputs of 8 MiB or more: a contiguous row-major A (n a multiple of
+    32) is read by the GPU straight from pageable memory where the device
+    reaches it (else page-locked for the call); other layouts take the staged
+    copy.  The solution equals the one from the device-resident factor and
+    solve bit for bit, and the caller's A is left untouched."""
+    rng = np.random.default_rng(n)
+    a0 = np.asarray(rng.standard_normal((n, n)), order=order)
+    keep = a0.copy(order="K")
+    b = rng.standard_normal((n, 16))
+    x = np.empty_like(b)
+    lib, ctx = _lib.load(), _lib.context()
+    rc = lib.luhot_dgesv(ctx, n, 16, a0.ctypes.data, a0.strides[0] // 8, a0.strides[1] // 8, b.ctypes.data, 16, 1,
+                         x.ctypes.data, 16, 1, 0)
+    _lib.check(rc, ctx)
+    assert np.array_equal(a0, keep)
+    a = np.ascontiguousarray(keep)
+    piv, _ = lapack.getrf(a)
+    np.testing.assert_array_equal(x, lapack.getrs(a, piv, b))
+
+
 def test_gesv_singular_status():
     lib, ctx = _lib.load(), _lib.context()
     a = np.ones((4, 4))
