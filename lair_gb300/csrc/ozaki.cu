@@ -30,29 +30,33 @@
 //   (built with integer operations) and one of the subtraction.  Rows or columns holding Inf or NaN give
 //   NaN in the elements they touch.
 //
-// oz_gemm_kernel: persistent, one CTA per SM, 128 x 128 output tiles in row
-// order, a contiguous range per CTA.  An M = 128 MMA costs the tensor pipe
-// about the same time for any N up to 256 (measured: ~128 cycles at N = 64),
-// so the tile is as wide as TMEM allows: two 128-column FP32 accumulators and
-// the 64-bit fixed-point sums of the 128 x 128 tile (256 columns).  Ten warps:
-//   warp 0      TMA producer: the seven 128-row A slices of the CTA's current
-//               row block (112 KB, reloaded when the row block changes) and
-//               the seven 128-row B slices of each tile (112 KB), one barrier
-//               pair per slice: slice q is last read by group G = q, so the
+// oz_gemm_kernel: persistent, one CTA per SM, 128 x 128 output tiles, a
+// contiguous range per CTA in column-block order.  An M = 128 MMA costs the
+// tensor pipe about the same time for any N up to 256 (measured: ~128 cycles
+// at N = 64), so the tile is as wide as TMEM allows: three 128-column FP32
+// accumulators and the low words of the tile's 64-bit fixed-point sums
+// (512 columns).  The MMAs compute C^T: TMEM lanes are C's columns, so a
+// warp's accesses to one row of C are 32 consecutive doubles.  Eighteen warps:
+//   warp 0      TMA producer: the seven U slices of the CTA's current column
+//               block (112 KB, reloaded when the column block changes) and
+//               the seven L slices of each tile (112 KB), one barrier pair
+//               per slice: L slice p is last read by group G = p, so the
 //               slices free up in the order the next tile needs them (6 .. 0);
 //               3-D tensor maps (k, row, slice), 128-byte swizzle, rows past M
 //               or N zero-filled;
 //   warp 1      TMEM owner (512 columns) and MMA issuer: per tile, groups
-//               G = 6 .. 0, taking the three accumulators in turn: the group's
-//               slice products, 4 k-steps of M = 128, N = 128, K = 16 each,
-//               then a commit to that accumulator's full barrier;
-//   warps 2-9   epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (tile
-//               rows) and 64 of the 128 columns ((w - 2) / 4): per group it
-//               folds the accumulator into the sums held in TMEM, 16 columns
-//               at a time, and releases the accumulator, so the MMAs of the
-//               next group (and of the next tile) overlap the epilogue; after
-//               group 0 it applies the sums to C (16-byte loads and stores,
-//               one FP64 subtraction per element).
+//               G = 6 .. 0, taking the three accumulators in turn over the
+//               launch: the group's slice products, 4 k-steps of M = 128,
+//               N = 128, K = 16 each, then a commit to that accumulator's full
+//               barrier;
+//   warps 2-17  epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (32
+//               columns of C) and 32 of the tile's 128 rows ((w - 2) / 4); its
+//               thread keeps the high words of its column's 32 sums in
+//               registers and the low words in TMEM; per group it folds the
+//               accumulator in (Horner on word pairs) and releases it, so the
+//               MMAs of the next group (and of the next tile) overlap the
+//               epilogue; after group 0 it applies the sums to C (C prefetched
+//               into L2 at the tile's start; one FP64 subtraction per element).
 // All mbarrier waits are bounded by the context's wait limit; on expiry a role
 // records the error and raises the CTA's abort flag, the others stop at their
 // next wait, and before exit the CTA waits (bounded) for its copies and MMAs
@@ -275,7 +279,7 @@ __device__ __forceinline__ void oz_tma3d(unsigned dst, const CUtensorMap* map, i
       : "memory");
 }
 
-// TMEM loads and stores of one warp: its 32 lanes, 4, 8, 16 or 32 consecutive
+// TMEM loads and stores of one warp: its 32 lanes, 4 or 16 consecutive
 // 32-bit columns from taddr (lane field in bits 16+).
 __device__ __forceinline__ void tmem_ld16(unsigned taddr, unsigned (&r)[16]) {
   asm volatile(
@@ -284,36 +288,10 @@ __device__ __forceinline__ void tmem_ld16(unsigned taddr, unsigned (&r)[16]) {
         "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
       : "r"(taddr));
 }
-__device__ __forceinline__ void tmem_ld32(unsigned taddr, unsigned (&r)[32]) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr));
-}
-__device__ __forceinline__ void tmem_st32(unsigned taddr, const unsigned (&r)[32]) {
-  asm volatile(
-      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,"
-      "%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};"
-      ::"r"(taddr), "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]),
-        "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15]), "r"(r[16]),
-        "r"(r[17]), "r"(r[18]), "r"(r[19]), "r"(r[20]), "r"(r[21]), "r"(r[22]), "r"(r[23]), "r"(r[24]),
-        "r"(r[25]), "r"(r[26]), "r"(r[27]), "r"(r[28]), "r"(r[29]), "r"(r[30]), "r"(r[31])
-      : "memory");
-}
 __device__ __forceinline__ void tmem_ld4(unsigned taddr, unsigned (&r)[4]) {
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
                : "r"(taddr));
-}
-__device__ __forceinline__ void tmem_ld8(unsigned taddr, unsigned (&r)[8]) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-      : "r"(taddr));
 }
 __device__ __forceinline__ void tmem_st16(unsigned taddr, const unsigned (&r)[16]) {
   asm volatile(
