@@ -46,3 +46,15 @@ def test_reference_arm_other_ranks_exit_quietly():
                       "--n", "256")
     assert r.returncode == 0, r.stderr[-2000:]
     assert json_lines(r.stdout) == []
+
+
+def test_roofline_traffic_comes_from_the_committed_profiles():
+    """The bench's roofline.traffic is the per-launch DRAM traffic of the
+    dominant kernel from its committed ncu summary (both update engines)."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    for name in ("oz_gemm_fp64_slices_n16384.md", "gemm_dmma_persistent_fp64_n16384.md"):
+        t = bench.read_traffic(os.path.join(ROOT, "profiles", name))
+        assert t is not None and t > 1e9, name
+    assert bench.read_traffic(os.path.join(ROOT, "profiles", "no_such_profile.md")) is None
