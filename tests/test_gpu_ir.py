@@ -89,6 +89,22 @@ def test_bf16x3_tensor_core_factor_with_plain_ir(kappa):
     assert berr(a, x1, b) <= 4 * berr(a, x2, b) + 1e-12
 
 
+def test_bf16x3_split_accumulators_keep_refinement_short():
+    """The BF16x3 update keeps its leading piece product apart from the five
+    small ones (separate TMEM accumulators), which makes the factor more
+    accurate as an FFMA FP32 one: plain IR at kappa = 1e6 needs about as many
+    corrections as with the FP32 factor (measured 4 and 4 here; 5 against 9
+    at n = 16384, where one accumulator took 14)."""
+    n = 2048
+    a = conditioned(n, 1e6, 21)
+    b = np.random.default_rng(22).standard_normal(n)
+    _, info3 = refine.gesv_ir(a, b, precision="bf16x3", solver="ir")
+    _, info32 = refine.gesv_ir(a, b, precision="fp32", solver="ir")
+    print(f"\nbf16x3: {info3['iterations']} corrections, fp32: {info32['iterations']}")
+    assert info3["converged"] == 1 and info32["converged"] == 1
+    assert info3["iterations"] <= info32["iterations"] + 1
+
+
 def test_tensor_core_plain_ir_small_kappa():
     n = 1536
     a = conditioned(n, 1e2, 15)
